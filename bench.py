@@ -1,0 +1,319 @@
+"""Benchmark: multi-stage bitruss peeling (msp) throughput on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload cl20m]
+
+Workload (default): the Chung-Lu power-law bipartite graph |U|=1,000,000,
+|V|=500,000, 20,000,000 unique edges, degree exponent 2.1 on both sides,
+degree cap 50,000, seed 2 (synthetic; see gpu_bitruss_gb300/gen.py).
+
+A step is one full msp decomposition of the resident graph through the C ABI
+(bt_msp: butterfly supports, then peeling to the bitruss number of every
+edge).  value = edges decomposed per second = m * K / (device time of the K
+timed steps), inputs resident in HBM.  Between timed steps L2 is flushed by
+writing a 512 MB buffer (and the graph arrays alone exceed the 129 MB L2).
+
+e2e: the same metric through the public API with host buffers: every step
+uploads the graph from host memory (H2D of offsets, degrees, neighbours, edge
+ids) and copies the m uint32 results back (D2H).
+
+roofline: the peeling kernel k_msp (the dominant kernel); achieved = its
+algorithmic bytes (counted by the kernel: 8 B per pivot slot walked (neighbour
++ edge id), 4 B per neighbour slot probed, 4 B per anchor slot staged, 8 B per
+butterfly found (two edge ids), 8 B per support decrement) / its CUDA-event
+time; peak = measured HBM copy bandwidth.
+
+cpu_baseline / --impl reference: the CPU restatement of the reference's
+algorithm (oracle/bt_oracle.c, OpenMP, all host cores) on a bounded sample of
+the same graph: butterfly supports of the whole graph, then peeling for a
+fixed time budget; edges peeled / elapsed time.
+
+Multi-GPU: msp does not shard (every sub-round needs the global frontier), so
+N > 1 runs N independent replicas, one per rank ("replicas only").
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "cl20m": "Chung-Lu bipartite |U|=1e6 |V|=5e5 m=2e7 gamma=2.1 cap=5e4 seed=2",
+    "cl1000k": "Chung-Lu bipartite |U|=5e4 |V|=2.5e4 m=1e6 gamma=2.1 seed=2 (scaled test case)",
+    "er": "Erdos-Renyi bipartite |U|=2000 |V|=3000 m=20000 seed=1",
+}
+L2_FLUSH_BYTES = 512 << 20
+METRIC = "msp bitruss edges/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(workload):
+    """DRAM bytes per k_msp launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_msp_traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get(workload)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_graph(workload: str):
+    from gpu_bitruss_gb300 import gen
+    import gpu_bitruss_gb300 as bt
+    u, v = gen.by_name(workload)
+    g = bt.Graph.from_edges(u, v)
+    return g, gen.digest(u, v)
+
+
+def cpu_sample(g, threads: int, budget_s: float):
+    """Oracle (reference algorithm restated) on a bounded sample of the graph:
+    supports of the whole graph + peeling for budget_s seconds."""
+    from oracle import oracle as O
+    d = g.as_dict()
+    t0 = time.perf_counter()
+    sup, _ = O.ebfc(d, threads)
+    _, _, st = O.msp(d, threads, O.MSP_TABLE, sup, max_seconds=budget_s)
+    dt = time.perf_counter() - t0
+    return st[3] / dt, st[3], dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    g, dig = make_graph(args.workload)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, peeled, dt = cpu_sample(g, threads, args.cpu_budget)
+        if i >= args.warmup:
+            vals.append((v, peeled, dt))
+    tot_e = sum(p for _, p, _ in vals)
+    tot_t = sum(t for _, _, t in vals)
+    value = tot_e / tot_t
+    sample = (f"oracle port, {threads} threads: supports of all {g.m} edges + peeling for "
+              f"{args.cpu_budget:.0f} s; {vals[-1][1]} edges peeled per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "edges/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "uint64", "data": "synthetic",
+        "config": {"workload": args.workload, "desc": WORKLOADS.get(args.workload, ""),
+                   "m": int(g.m), "graph_digest": dig, "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import gpu_bitruss_gb300 as bt
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    g, dig = make_graph(args.workload)
+    m = int(g.m)
+    ctx = bt.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload(g)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warm-up
+    for _ in range(args.warmup):
+        ctx.msp(out=False)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    total_ms, peel_ms, work = 0.0, [], None
+    launches = 0
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        ctx.msp(out=False)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        peel_ms.append(ctx.phase_ms("peel"))
+        st = ctx.stats()
+        work = st[8:14]
+        launches += 5  # k_count, k_msp_init, k_two_hop, k_msp, k_msp_result
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    stats = ctx.stats()
+    t_max = total_ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * m * args.steps / (t_max / 1000.0)
+
+    # e2e through the public API: H2D upload + msp + D2H of the results
+    out = np.zeros(m, np.uint32)
+    h2d = 4 * (g.n + 1) + 4 * g.n + 8 * m + 8 * m
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.upload(g)
+        b, _ = ctx.msp(out=True)
+        e2e_ms += 1000 * (time.perf_counter() - t0)
+    e2e_value = world * m * args.steps / (e2e_ms / 1000.0)
+
+    # roofline of k_msp
+    mids, probes, anchor, hits, decs = work[:5]
+    alg_bytes = 8 * mids + 4 * probes + 4 * anchor + 8 * hits + 8 * decs
+    t_peel = statistics.median(peel_ms) / 1000.0
+    achieved = alg_bytes / t_peel / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = load_traffic(args.workload)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "uint64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "desc": WORKLOADS.get(args.workload, ""),
+                   "m": m, "n": int(g.n), "graph_digest": dig, "parallelism": "replicas",
+                   "l2": "512 MB flush between timed steps; graph arrays > L2",
+                   "levels": stats[0], "subrounds": stats[1], "tasks": stats[3],
+                   "peel_ms": statistics.median(peel_ms), "ebfc_ms": ctx.phase_ms("ebfc")},
+        "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(4 * m)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} hbm_gbs", "kernel": "k_msp",
+                     "algorithmic_bytes": int(alg_bytes),
+                     "work": {"pivot_slots": mids, "probes": probes, "anchor_slots": anchor,
+                              "butterflies": hits, "decrements": decs}},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        v, peeled, dt = cpu_sample(g, os.cpu_count() or 1, args.cpu_budget)
+        line["cpu_baseline"] = {
+            "value": v, "unit": "edges/s", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"oracle port: supports of all {m} edges + peeling for "
+                      f"{args.cpu_budget:.0f} s ({peeled} edges peeled in {dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cl20m", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

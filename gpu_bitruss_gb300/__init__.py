@@ -1,0 +1,323 @@
+"""GB300 bitruss engine: Python mirror of the reference's host interface.
+
+The engine is ``libbitruss.so`` (C ABI in ``include/bitruss.h``; CUDA kernels
+for sm_103a).  This module binds it with ctypes and keeps the reference's
+names (``src/graph/graph.h:30-52``, ``src/bfc/bfc.cuh:18-19``,
+``src/bitruss/bitruss.cuh:17-18``):
+
+    g = Graph.from_text("g.txt")          # Graph(path, true) / process_graph
+    g.to_bin("g.bin")                      # graph_to_bin
+    g = Graph.from_bin("g.bin")            # Graph(path, false) / load_graph_bin
+    bfc_vpp(g)            -> g.butterflies
+    bfc_evpp(g)           -> g.edge_support (uint64), g.support_max
+    g_bitruss_hindex(g)   -> g.bitruss (uint32), g.rounds
+    bitruss_msp(g)        -> g.bitruss (uint32), g.levels
+
+Failures raise ``BitrussError`` (the reference calls exit()).  There is no CPU
+fallback: without the built library or a GB300 the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "BitrussError", "Graph", "Context", "load", "build",
+    "bfc_vpp", "bfc_evpp", "g_bitruss_hindex", "bitruss_msp", "bitruss_msp_exact",
+    "STATUS", "SYMBOLS",
+]
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libbitruss.so")
+COH_PATH = os.path.join(PKG, "coh")
+
+STATUS = {
+    0: "BT_OK", 1: "BT_ERR_INVALID", 2: "BT_ERR_IO", 3: "BT_ERR_FORMAT",
+    4: "BT_ERR_HOST_MEMORY", 5: "BT_ERR_DEVICE_MEMORY", 6: "BT_ERR_CUDA",
+    7: "BT_ERR_TIMEOUT", 8: "BT_ERR_STATE", 9: "BT_ERR_NO_DEVICE", 10: "BT_ERR_OVERFLOW",
+}
+
+# every symbol include/bitruss.h declares
+SYMBOLS = [
+    "bt_graph_load_bin", "bt_graph_load_text", "bt_graph_from_edges", "bt_graph_save_bin",
+    "bt_graph_get_view", "bt_graph_free", "bt_ctx_create", "bt_ctx_set_stream",
+    "bt_ctx_set_memory_budget", "bt_ctx_memory_used", "bt_ctx_free", "bt_graph_upload",
+    "bt_bfc", "bt_ebfc", "bt_hidx", "bt_msp", "bt_msp_exact", "bt_result_download",
+    "bt_ctx_phase_ms", "bt_ctx_stats", "bt_status_string", "bt_last_error",
+]
+
+
+class BitrussError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str):
+        self.status = status
+        self.code = STATUS.get(status, str(status))
+        super().__init__(f"{where}: {self.code}: {message}")
+
+
+class _View(C.Structure):
+    _fields_ = [
+        ("u_num", C.c_uint32), ("l_num", C.c_uint32), ("u_max", C.c_uint32), ("n", C.c_uint32),
+        ("m", C.c_uint64), ("support_max", C.c_uint64),
+        ("offsets", C.c_void_p), ("neighbors", C.c_void_p), ("degrees", C.c_void_p),
+        ("edges", C.c_void_p), ("edge_ids", C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def build(verbose: bool = False) -> str:
+    from . import _build
+    return _build.build(verbose=verbose)
+
+
+def load():
+    """Load libbitruss.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise BitrussError(9, "load", f"{LIB_PATH} is missing: build it with "
+                           "gpu_bitruss_gb300.build() (nvcc for sm_103a)")
+    L = C.CDLL(LIB_PATH)
+    P, u32, u64, i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+    sig = {
+        "bt_graph_load_bin": ([C.c_char_p, C.POINTER(P)], i32),
+        "bt_graph_load_text": ([C.c_char_p, C.POINTER(P)], i32),
+        "bt_graph_from_edges": ([P, P, u64, C.POINTER(P)], i32),
+        "bt_graph_save_bin": ([P, C.c_char_p], i32),
+        "bt_graph_get_view": ([P, C.POINTER(_View)], i32),
+        "bt_graph_free": ([P], None),
+        "bt_ctx_create": ([i32, C.POINTER(P)], i32),
+        "bt_ctx_set_stream": ([P, P], i32),
+        "bt_ctx_set_memory_budget": ([P, u64], i32),
+        "bt_ctx_memory_used": ([P, C.POINTER(u64)], i32),
+        "bt_ctx_free": ([P], None),
+        "bt_graph_upload": ([P, P], i32),
+        "bt_bfc": ([P, C.POINTER(u64)], i32),
+        "bt_ebfc": ([P, P, C.POINTER(u64), C.POINTER(u64)], i32),
+        "bt_hidx": ([P, P, C.POINTER(u32)], i32),
+        "bt_msp": ([P, P, C.POINTER(u32)], i32),
+        "bt_msp_exact": ([P, P, C.POINTER(u32)], i32),
+        "bt_result_download": ([P, P, C.c_size_t], i32),
+        "bt_ctx_phase_ms": ([P, C.c_char_p], C.c_double),
+        "bt_ctx_stats": ([P, C.POINTER(u64), i32], i32),
+        "bt_status_string": ([i32], C.c_char_p),
+        "bt_last_error": ([], C.c_char_p),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int, where: str) -> None:
+    if rc != 0:
+        msg = load().bt_last_error().decode(errors="replace")
+        raise BitrussError(rc, where, msg)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Graph:
+    """Host CSR in the reference layout (graph.h:43-51)."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self.edge_support = None   # np.uint64[m] after bfc_evpp
+        self.bitruss = None        # np.uint32[m] after hidx / msp
+        self.butterflies = None
+        self.levels = None
+        self.rounds = None
+        self._refresh()
+
+    # constructors -------------------------------------------------------
+    @classmethod
+    def from_edges(cls, u, v) -> "Graph":
+        u = np.ascontiguousarray(u, dtype=np.uint32)
+        v = np.ascontiguousarray(v, dtype=np.uint32)
+        if u.shape != v.shape:
+            raise ValueError("u and v differ in length")
+        h = C.c_void_p()
+        _check(load().bt_graph_from_edges(_ptr(u), _ptr(v), u.size, C.byref(h)), "process_graph")
+        return cls(h)
+
+    @classmethod
+    def from_text(cls, path: str) -> "Graph":
+        h = C.c_void_p()
+        _check(load().bt_graph_load_text(path.encode(), C.byref(h)), "process_graph")
+        return cls(h)
+
+    @classmethod
+    def from_bin(cls, path: str) -> "Graph":
+        h = C.c_void_p()
+        _check(load().bt_graph_load_bin(path.encode(), C.byref(h)), "load_graph_bin")
+        return cls(h)
+
+    def to_bin(self, path: str) -> None:
+        _check(load().bt_graph_save_bin(self._h, path.encode()), "graph_to_bin")
+
+    graph_to_bin = to_bin
+
+    def _refresh(self):
+        v = _View()
+        _check(load().bt_graph_get_view(self._h, C.byref(v)), "graph view")
+        self.u_num, self.l_num, self.u_max, self.n, self.m = v.u_num, v.l_num, v.u_max, v.n, v.m
+        self.support_max = v.support_max
+
+        def arr(p, k):
+            if k == 0 or not p:
+                return np.zeros(0, np.uint32)
+            return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint32)), shape=(k,))
+
+        self.offsets = arr(v.offsets, self.n + 1)
+        self.neighbors = arr(v.neighbors, 2 * self.m)
+        self.degrees = arr(v.degrees, self.n)
+        self.edges = arr(v.edges, 2 * self.m)
+        self.edge_ids = arr(v.edge_ids, 2 * self.m)
+
+    def as_dict(self) -> dict:
+        """Arrays as a dict (the layout the CPU oracle takes)."""
+        return {"u_num": self.u_num, "l_num": self.l_num, "n": self.n, "m": self.m,
+                "offsets": self.offsets, "degrees": self.degrees, "neighbors": self.neighbors,
+                "edges": self.edges, "edge_ids": self.edge_ids}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bt_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """A device context: one stream, one resident graph."""
+
+    def __init__(self, device: int = 0):
+        self._c = C.c_void_p()
+        _check(load().bt_ctx_create(device, C.byref(self._c)), "bt_ctx_create")
+        self.graph = None
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _check(load().bt_ctx_set_stream(self._c, C.c_void_p(stream_ptr or 0)), "set_stream")
+
+    def set_budget(self, nbytes: int) -> None:
+        _check(load().bt_ctx_set_memory_budget(self._c, nbytes), "set_budget")
+
+    def memory_used(self) -> int:
+        x = C.c_uint64()
+        _check(load().bt_ctx_memory_used(self._c, C.byref(x)), "memory_used")
+        return x.value
+
+    def upload(self, g: Graph) -> None:
+        _check(load().bt_graph_upload(self._c, g._h), "graph upload")
+        self.graph = g
+
+    def bfc(self) -> int:
+        c = C.c_uint64()
+        _check(load().bt_bfc(self._c, C.byref(c)), "bfc_vpp")
+        return c.value
+
+    def ebfc(self, out: bool = True):
+        m = self.graph.m
+        sup = np.zeros(m, np.uint64) if out else None
+        c, mx = C.c_uint64(), C.c_uint64()
+        _check(load().bt_ebfc(self._c, _ptr(sup) if m else None, C.byref(c), C.byref(mx)), "bfc_evpp")
+        return sup, c.value, mx.value
+
+    def hidx(self, out: bool = True):
+        m = self.graph.m
+        b = np.zeros(m, np.uint32) if out else None
+        r = C.c_uint32()
+        _check(load().bt_hidx(self._c, _ptr(b) if m else None, C.byref(r)), "g_bitruss_hindex")
+        return b, r.value
+
+    def msp(self, exact: bool = False, out: bool = True):
+        m = self.graph.m
+        b = np.zeros(m, np.uint32) if out else None
+        lv = C.c_uint32()
+        f = load().bt_msp_exact if exact else load().bt_msp
+        _check(f(self._c, _ptr(b) if m else None, C.byref(lv)), "bitruss_msp")
+        return b, lv.value
+
+    def download(self, out: np.ndarray) -> None:
+        _check(load().bt_result_download(self._c, _ptr(out), out.nbytes), "result download")
+
+    def phase_ms(self, phase: str) -> float:
+        return float(load().bt_ctx_phase_ms(self._c, phase.encode()))
+
+    def stats(self) -> list[int]:
+        """[levels, sub-rounds, compressions, tasks, hidx rounds, non-empty
+        levels, bucket splits, -, pivot slots, probes, anchor slots,
+        butterflies found, decrements, m, -, -]"""
+        a = (C.c_uint64 * 16)()
+        _check(load().bt_ctx_stats(self._c, a, 16), "stats")
+        return list(a)
+
+    def close(self):
+        if getattr(self, "_c", None):
+            load().bt_ctx_free(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Context | None = None
+
+
+def _ctx_for(g: Graph) -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    if _default_ctx.graph is not g:
+        _default_ctx.upload(g)
+    return _default_ctx
+
+
+def bfc_vpp(g: Graph) -> int:
+    """Global butterfly count (bfc_vpp.cu:321-385)."""
+    g.butterflies = _ctx_for(g).bfc()
+    return g.butterflies
+
+
+def bfc_evpp(g: Graph) -> np.ndarray:
+    """Per-edge butterfly support (bfc_vpp.cu:233-309)."""
+    sup, c, mx = _ctx_for(g).ebfc()
+    g.edge_support, g.butterflies, g.support_max = sup, c, mx
+    return sup
+
+
+def g_bitruss_hindex(g: Graph) -> np.ndarray:
+    """Bitruss numbers by h-index iteration (bitruss_hidx.cu:179-256)."""
+    b, r = _ctx_for(g).hidx()
+    g.bitruss, g.rounds = b, r
+    return b
+
+
+def bitruss_msp(g: Graph) -> np.ndarray:
+    """Bitruss numbers by multi-stage peeling (bitruss_msp.cu:440-583)."""
+    b, lv = _ctx_for(g).msp()
+    g.bitruss, g.levels = b, lv
+    return b
+
+
+def bitruss_msp_exact(g: Graph) -> np.ndarray:
+    """Peeling with the corrected one-survivor rule (equals hidx)."""
+    b, lv = _ctx_for(g).msp(exact=True)
+    g.bitruss, g.levels = b, lv
+    return b

@@ -1,0 +1,469 @@
+// bt_ctx.cu -- device context, device arena, graph upload and the C ABI.
+//
+// Upload replaces the per-call cudaMalloc + cudaMemcpy of the reference's
+// host drivers (bfc_vpp.cu:245-267, bitruss_msp.cu:453-465,
+// bitruss_hidx.cu:196-211): the graph is copied once and stays resident.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+#include <cub/device/device_segmented_sort.cuh>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "bt_internal.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string t_last_error;
+
+bt_status bt_fail(bt_status s, const std::string &msg) {
+    t_last_error = msg;
+    return s;
+}
+
+bt_status bt_cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+    cudaGetLastError();  // clear a non-sticky error
+    std::string msg = std::string(cudaGetErrorName(e)) + " (" + cudaGetErrorString(e) + ") in " +
+                      what + " at " + file + ":" + std::to_string(line);
+    if (e == cudaErrorMemoryAllocation) return bt_fail(BT_ERR_DEVICE_MEMORY, msg);
+    if (e == cudaErrorNoDevice || e == cudaErrorInvalidDevice || e == cudaErrorNoKernelImageForDevice ||
+        e == cudaErrorInsufficientDriver)
+        return bt_fail(BT_ERR_NO_DEVICE, msg);
+    return bt_fail(BT_ERR_CUDA, msg);
+}
+
+extern "C" const char *bt_last_error(void) { return t_last_error.c_str(); }
+
+extern "C" const char *bt_status_string(bt_status s) {
+    switch (s) {
+        case BT_OK: return "ok";
+        case BT_ERR_INVALID: return "invalid argument";
+        case BT_ERR_IO: return "i/o error";
+        case BT_ERR_FORMAT: return "malformed input";
+        case BT_ERR_HOST_MEMORY: return "host out of memory";
+        case BT_ERR_DEVICE_MEMORY: return "device out of memory or over budget";
+        case BT_ERR_CUDA: return "CUDA error";
+        case BT_ERR_TIMEOUT: return "device wait timed out";
+        case BT_ERR_STATE: return "call out of order";
+        case BT_ERR_NO_DEVICE: return "no usable CUDA device";
+        case BT_ERR_OVERFLOW: return "result overflows its output type";
+    }
+    return "unknown status";
+}
+
+// ---------------------------------------------------------------------------
+// device arena
+// ---------------------------------------------------------------------------
+
+bt_status ctx_alloc(bt_ctx *ctx, void **p, uint64_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    bytes = (bytes + 255) & ~255ull;
+    if (ctx->budget && ctx->used + bytes > ctx->budget)
+        return bt_fail(BT_ERR_DEVICE_MEMORY, "device budget of " + std::to_string(ctx->budget) +
+                                                 " bytes exceeded (need " +
+                                                 std::to_string(ctx->used + bytes) + ")");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return bt_cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+    }
+    ctx->used += bytes;
+    ctx->allocs.emplace_back(*p, bytes);
+    return BT_OK;
+}
+
+void ctx_free(bt_ctx *ctx, void *p) {
+    if (!p) return;
+    for (size_t i = 0; i < ctx->allocs.size(); i++) {
+        if (ctx->allocs[i].first == p) {
+            ctx->used -= ctx->allocs[i].second;
+            ctx->allocs.erase(ctx->allocs.begin() + (long)i);
+            break;
+        }
+    }
+    cudaFree(p);
+}
+
+bt_status ctx_scratch(bt_ctx *ctx, uint64_t bytes, void **p) {
+    if (ctx->scratch_bytes < bytes) {
+        ctx_free(ctx, ctx->scratch);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+        BT_TRY(ctx_alloc(ctx, &ctx->scratch, bytes));
+        ctx->scratch_bytes = bytes;
+    }
+    *p = ctx->scratch;
+    return BT_OK;
+}
+
+void ctx_release_graph(bt_ctx *ctx) {
+    DevGraph &g = ctx->g;
+    ctx_free(ctx, g.off);
+    ctx_free(ctx, g.deg0);
+    ctx_free(ctx, g.nbr0);
+    ctx_free(ctx, g.eid0);
+    ctx_free(ctx, g.ends);
+    ctx_free(ctx, g.is_u);
+    ctx_free(ctx, ctx->sup);
+    ctx_free(ctx, ctx->result);
+    ctx->sup = nullptr;
+    ctx->result = nullptr;
+    g = DevGraph();
+    ctx->has_graph = false;
+    ctx->last_result = 0;
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+
+extern "C" bt_status bt_ctx_create(int device, bt_ctx **out) {
+    if (!out) return bt_fail(BT_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return bt_fail(BT_ERR_NO_DEVICE, "no CUDA device available");
+    if (device < 0 || device >= count)
+        return bt_fail(BT_ERR_NO_DEVICE, "gpu device id " + std::to_string(device) + " is not available");
+    BT_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    BT_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3)
+        return bt_fail(BT_ERR_NO_DEVICE, std::string("device ") + prop.name + " is sm_" +
+                                             std::to_string(prop.major) + std::to_string(prop.minor) +
+                                             "; this build targets sm_103a (GB300)");
+    bt_ctx *ctx = new (std::nothrow) bt_ctx();
+    if (!ctx) return bt_fail(BT_ERR_HOST_MEMORY, "host allocation failed");
+    ctx->device = device;
+    ctx->sm_count = prop.multiProcessorCount;
+    e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return bt_cuda_fail(e, "cudaStreamCreate", __FILE__, __LINE__);
+    }
+    ctx->stream = ctx->own_stream;
+    for (auto &ev : ctx->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return BT_OK;
+}
+
+extern "C" bt_status bt_ctx_set_stream(bt_ctx *ctx, void *stream) {
+    if (!ctx) return bt_fail(BT_ERR_INVALID, "null context");
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return BT_OK;
+}
+
+extern "C" bt_status bt_ctx_set_memory_budget(bt_ctx *ctx, uint64_t bytes) {
+    if (!ctx) return bt_fail(BT_ERR_INVALID, "null context");
+    ctx->budget = bytes;
+    return BT_OK;
+}
+
+extern "C" bt_status bt_ctx_memory_used(const bt_ctx *ctx, uint64_t *bytes) {
+    if (!ctx || !bytes) return bt_fail(BT_ERR_INVALID, "null argument");
+    *bytes = ctx->used;
+    return BT_OK;
+}
+
+extern "C" void bt_ctx_free(bt_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    while (!ctx->allocs.empty()) ctx_free(ctx, ctx->allocs.back().first);
+    for (auto &ev : ctx->ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+extern "C" double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase) {
+    if (!ctx || !phase) return -1;
+    static const char *names[] = {"upload", "ebfc", "peel", "hidx", "total", "msp"};
+    for (int i = 0; i < 6; i++)
+        if (!strcmp(phase, names[i])) return ctx->phase_ms[i];
+    return -1;
+}
+
+extern "C" bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n) {
+    if (!ctx || !out) return bt_fail(BT_ERR_INVALID, "null argument");
+    for (int i = 0; i < n && i < 8; i++) out[i] = ctx->stats[i];
+    for (int i = 8; i < n && i < 16; i++) out[i] = ctx->work[i - 8];
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// graph upload: reference CSR -> rank-relabelled device CSR
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// priority sort key: ascending key = descending (degree, id)
+__global__ void k_rank_keys(uint32_t n, const uint32_t *deg, unsigned long long *key, uint32_t *val) {
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        key[x] = ((unsigned long long)(0xffffffffu - deg[x]) << 32) | (0xffffffffu - x);
+        val[x] = x;
+    }
+}
+
+__global__ void k_rank_scatter(uint32_t n, uint32_t u_num, const uint32_t *order, const uint32_t *deg,
+                               uint32_t *rank, uint32_t *deg_r, uint32_t *is_u) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t x = order[i];
+        rank[x] = i;
+        deg_r[i] = deg[x];
+        is_u[i] = x < u_num ? 1u : 0u;
+    }
+}
+
+// copy each row into its rank position, mapping neighbour ids to ranks;
+// one warp per vertex
+__global__ void k_rows_relabel(uint32_t n, uint32_t u_num, const uint32_t *off, const uint32_t *nbr,
+                               const uint32_t *eid, const uint32_t *rank, const uint32_t *off_r,
+                               uint32_t *nbr_r, uint32_t *eid_r, uint2 *ends) {
+    uint32_t lane = threadIdx.x & 31;
+    uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t x = warp; x < n; x += nwarps) {
+        uint32_t b = off[x], len = off[x + 1] - b, rx = rank[x], dst = off_r[rx];
+        for (uint32_t j = lane; j < len; j += 32) {
+            uint32_t y = nbr[b + j], e = eid[b + j], ry = rank[y];
+            nbr_r[dst + j] = ry;
+            eid_r[dst + j] = e;
+            if (x < u_num) ends[e] = make_uint2(rx, ry);
+        }
+    }
+}
+
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap) {
+    uint64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+}  // namespace
+
+bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
+    ctx_release_graph(ctx);
+    DevGraph &g = ctx->g;
+    cudaStream_t st = ctx->stream;
+    uint32_t n = hg->n;
+    uint64_t m = hg->m;
+    g.n = n;
+    g.m = m;
+    g.u_num = hg->u_num;
+    uint32_t maxd = 0;
+    for (uint32_t x = 0; x < n; x++) maxd = hg->degrees[x] > maxd ? hg->degrees[x] : maxd;
+    g.max_deg = maxd;
+
+    // persistent arrays
+    BT_TRY(ctx_alloc_t(ctx, &g.off, (uint64_t)n + 1));
+    BT_TRY(ctx_alloc_t(ctx, &g.deg0, n));
+    BT_TRY(ctx_alloc_t(ctx, &g.nbr0, 2 * m));
+    BT_TRY(ctx_alloc_t(ctx, &g.eid0, 2 * m));
+    BT_TRY(ctx_alloc_t(ctx, &g.ends, m));
+    BT_TRY(ctx_alloc_t(ctx, &g.is_u, n));
+    BT_TRY(ctx_alloc_t(ctx, &ctx->sup, m));
+    BT_TRY(ctx_alloc_t(ctx, &ctx->result, m));
+
+    // staging: reference CSR on device (freed at the end)
+    uint32_t *s_off = nullptr, *s_nbr = nullptr, *s_eid = nullptr, *s_deg = nullptr;
+    uint32_t *rank = nullptr, *order = nullptr, *vals = nullptr, *t_nbr = nullptr, *t_eid = nullptr;
+    unsigned long long *keys = nullptr, *keys2 = nullptr;
+    void *temp = nullptr;
+    bt_status rc = BT_OK;
+    auto cleanup = [&]() {
+        ctx_free(ctx, s_off); ctx_free(ctx, s_nbr); ctx_free(ctx, s_eid); ctx_free(ctx, s_deg);
+        ctx_free(ctx, rank); ctx_free(ctx, order); ctx_free(ctx, vals);
+        ctx_free(ctx, t_nbr); ctx_free(ctx, t_eid);
+        ctx_free(ctx, keys); ctx_free(ctx, keys2); ctx_free(ctx, temp);
+    };
+#define STEP(x)                 \
+    do {                        \
+        rc = (x);               \
+        if (rc != BT_OK) {      \
+            cleanup();          \
+            return rc;          \
+        }                       \
+    } while (0)
+#define STEPC(x)                                                          \
+    do {                                                                  \
+        cudaError_t _e = (x);                                             \
+        if (_e != cudaSuccess) {                                          \
+            cleanup();                                                    \
+            return bt_cuda_fail(_e, #x, __FILE__, __LINE__);              \
+        }                                                                 \
+    } while (0)
+
+    STEP(ctx_alloc_t(ctx, &s_off, (uint64_t)n + 1));
+    STEP(ctx_alloc_t(ctx, &s_deg, n));
+    STEP(ctx_alloc_t(ctx, &s_nbr, 2 * m));
+    STEP(ctx_alloc_t(ctx, &s_eid, 2 * m));
+    STEP(ctx_alloc_t(ctx, &rank, n));
+    STEP(ctx_alloc_t(ctx, &order, n));
+    STEP(ctx_alloc_t(ctx, &vals, n));
+    STEP(ctx_alloc_t(ctx, &keys, n));
+    STEP(ctx_alloc_t(ctx, &keys2, n));
+    STEP(ctx_alloc_t(ctx, &t_nbr, 2 * m));
+    STEP(ctx_alloc_t(ctx, &t_eid, 2 * m));
+
+    STEPC(cudaMemcpyAsync(s_off, hg->offsets.data(), 4 * ((uint64_t)n + 1), cudaMemcpyHostToDevice, st));
+    STEPC(cudaMemcpyAsync(s_deg, hg->degrees.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+    if (m) {
+        STEPC(cudaMemcpyAsync(s_nbr, hg->neighbors.data(), 8 * m, cudaMemcpyHostToDevice, st));
+        STEPC(cudaMemcpyAsync(s_eid, hg->edge_ids.data(), 8 * m, cudaMemcpyHostToDevice, st));
+    }
+
+    // temp storage for the cub calls (max over the three)
+    size_t t1 = 0, t2 = 0, t3 = 0;
+    STEPC(cub::DeviceRadixSort::SortPairs(nullptr, t1, keys, keys2, vals, order, (int)n, 0, 64, st));
+    STEPC(cub::DeviceScan::ExclusiveSum(nullptr, t2, g.deg0, g.off, (int)n + 1, st));
+    STEPC(cub::DeviceSegmentedSort::SortPairs(nullptr, t3, t_nbr, g.nbr0, t_eid, g.eid0, (int64_t)(2 * m),
+                                              (int64_t)n, g.off, g.off + 1, st));
+    size_t tb = t1 > t2 ? t1 : t2;
+    tb = tb > t3 ? tb : t3;
+    STEP(ctx_alloc(ctx, &temp, tb));
+
+    unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
+    if (n) {
+        k_rank_keys<<<grid_for(n, blk, cap), blk, 0, st>>>(n, s_deg, keys, vals);
+        STEPC(cub::DeviceRadixSort::SortPairs(temp, t1, keys, keys2, vals, order, (int)n, 0, 64, st));
+        k_rank_scatter<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.u_num, order, s_deg, rank, g.deg0, g.is_u);
+    }
+    // off = exclusive scan of deg0 over n+1 entries (deg0[n] read as garbage is
+    // avoided by scanning n entries and setting off[n] = 2m)
+    STEPC(cub::DeviceScan::ExclusiveSum(temp, t2, g.deg0, g.off, (int)n, st));
+    {
+        uint32_t total = (uint32_t)(2 * m);
+        STEPC(cudaMemcpyAsync(g.off + n, &total, 4, cudaMemcpyHostToDevice, st));
+        STEPC(cudaStreamSynchronize(st));  // `total` lives on the host stack
+    }
+    if (n) {
+        k_rows_relabel<<<grid_for((uint64_t)n * 32, blk, cap), blk, 0, st>>>(n, g.u_num, s_off, s_nbr, s_eid,
+                                                                              rank, g.off, t_nbr, t_eid, g.ends);
+        STEPC(cudaGetLastError());
+    }
+    if (m) {
+        STEPC(cub::DeviceSegmentedSort::SortPairs(temp, t3, t_nbr, g.nbr0, t_eid, g.eid0, (int64_t)(2 * m),
+                                                  (int64_t)n, g.off, g.off + 1, st));
+    }
+    STEPC(cudaStreamSynchronize(st));
+    cleanup();
+#undef STEP
+#undef STEPC
+    ctx->has_graph = true;
+    ctx->u_max = hg->u_max;
+    ctx->l_num = hg->l_num;
+    ctx->last_result = 0;
+    return BT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI: upload and algorithms
+// ---------------------------------------------------------------------------
+
+static bt_status enter(bt_ctx *ctx) {
+    if (!ctx) return bt_fail(BT_ERR_INVALID, "null context");
+    BT_CUDA(cudaSetDevice(ctx->device));
+    return BT_OK;
+}
+
+static bt_status need_graph(bt_ctx *ctx) {
+    BT_TRY(enter(ctx));
+    if (!ctx->has_graph) return bt_fail(BT_ERR_STATE, "no graph uploaded to this context");
+    return BT_OK;
+}
+
+static void time_begin(bt_ctx *ctx) { cudaEventRecord(ctx->ev[0], ctx->stream); }
+static void time_end(bt_ctx *ctx, int phase) {
+    cudaEventRecord(ctx->ev[1], ctx->stream);
+    cudaEventSynchronize(ctx->ev[1]);
+    float ms = -1;
+    if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) ctx->phase_ms[phase] = ms;
+}
+
+extern "C" bt_status bt_graph_upload(bt_ctx *ctx, const bt_graph *g) {
+    BT_TRY(enter(ctx));
+    if (!g) return bt_fail(BT_ERR_INVALID, "null graph");
+    time_begin(ctx);
+    BT_TRY(dev_build_graph(ctx, g));
+    time_end(ctx, PH_UPLOAD);
+    return BT_OK;
+}
+
+static bt_status copy_out(bt_ctx *ctx, void *host, const void *dev, uint64_t bytes) {
+    if (!host || bytes == 0) return BT_OK;
+    BT_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return BT_OK;
+}
+
+extern "C" bt_status bt_bfc(bt_ctx *ctx, uint64_t *count) {
+    BT_TRY(need_graph(ctx));
+    time_begin(ctx);
+    uint64_t c = 0;
+    BT_TRY(dev_ebfc(ctx, false, &c));
+    time_end(ctx, PH_TOTAL);
+    if (count) *count = c;
+    return BT_OK;
+}
+
+extern "C" bt_status bt_ebfc(bt_ctx *ctx, uint64_t *sup, uint64_t *count, uint64_t *support_max) {
+    BT_TRY(need_graph(ctx));
+    time_begin(ctx);
+    uint64_t c = 0;
+    BT_TRY(dev_ebfc(ctx, true, &c));
+    time_end(ctx, PH_TOTAL);
+    if (count) *count = c;
+    if (support_max) *support_max = ctx->last_sup_max;
+    return copy_out(ctx, sup, ctx->sup, 8 * ctx->g.m);
+}
+
+extern "C" bt_status bt_msp(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels) {
+    BT_TRY(need_graph(ctx));
+    time_begin(ctx);
+    uint32_t lv = 0;
+    BT_TRY(dev_msp(ctx, false, &lv));
+    time_end(ctx, PH_TOTAL);
+    if (levels) *levels = lv;
+    return copy_out(ctx, bitruss, ctx->result, 4 * ctx->g.m);
+}
+
+extern "C" bt_status bt_msp_exact(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels) {
+    BT_TRY(need_graph(ctx));
+    time_begin(ctx);
+    uint32_t lv = 0;
+    BT_TRY(dev_msp(ctx, true, &lv));
+    time_end(ctx, PH_TOTAL);
+    if (levels) *levels = lv;
+    return copy_out(ctx, bitruss, ctx->result, 4 * ctx->g.m);
+}
+
+extern "C" bt_status bt_hidx(bt_ctx *ctx, uint32_t *bitruss, uint32_t *rounds) {
+    BT_TRY(need_graph(ctx));
+    time_begin(ctx);
+    uint32_t r = 0;
+    BT_TRY(dev_hidx(ctx, &r));
+    time_end(ctx, PH_TOTAL);
+    if (rounds) *rounds = r;
+    return copy_out(ctx, bitruss, ctx->result, 4 * ctx->g.m);
+}
+
+extern "C" bt_status bt_result_download(bt_ctx *ctx, void *host, size_t bytes) {
+    BT_TRY(need_graph(ctx));
+    if (!host) return bt_fail(BT_ERR_INVALID, "null host buffer");
+    if (ctx->last_result == 1) {
+        if (bytes < 8 * ctx->g.m) return bt_fail(BT_ERR_INVALID, "buffer smaller than m uint64");
+        return copy_out(ctx, host, ctx->sup, 8 * ctx->g.m);
+    }
+    if (ctx->last_result == 2) {
+        if (bytes < 4 * ctx->g.m) return bt_fail(BT_ERR_INVALID, "buffer smaller than m uint32");
+        return copy_out(ctx, host, ctx->result, 4 * ctx->g.m);
+    }
+    return bt_fail(BT_ERR_STATE, "no result on this context");
+}

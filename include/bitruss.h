@@ -1,0 +1,157 @@
+/*
+ * bitruss.h -- C ABI of the GB300 bitruss engine (libbitruss.so).
+ *
+ * Drop-in for the GPU path of ShunyangLi/GPU_Bitruss
+ * (`coh --gpu --algo bfc|ebfc|hidx|msp`).  Each entry point names the
+ * reference interface it replaces.  All sizes are in elements unless stated;
+ * every call returns a bt_status and never exits the process (the reference
+ * calls exit(EXIT_FAILURE) on any CUDA error: src/util/utility.h:52-62).
+ *
+ * Data contract (reference layout, src/graph/graph.h:43-51):
+ *   vertex ids   uint32; U vertices 0..u_num-1, V vertices u_num..n-1
+ *   edge id e    rank of the edge in U-major order with sorted rows
+ *                (src/graph/graph.cpp:178-194); edges[2e]=U end, edges[2e+1]=V end
+ *   supports     uint64 per edge (the reference's int32 overflows on hub-hub
+ *                edges of power-law graphs)
+ *   bitruss      uint32 per edge
+ *   butterflies  uint64 total
+ *
+ * Threading: one bt_ctx per host thread.  A context owns one CUDA stream and
+ * the device-resident copy of one graph; calls on a context are synchronous
+ * with respect to the host (they return when the result is ready).
+ */
+#ifndef BITRUSS_GB300_H
+#define BITRUSS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    BT_OK = 0,
+    BT_ERR_INVALID = 1,     /* bad argument or malformed input            */
+    BT_ERR_IO = 2,          /* file could not be opened / read / written  */
+    BT_ERR_FORMAT = 3,      /* .bin header or size inconsistent           */
+    BT_ERR_HOST_MEMORY = 4, /* host allocation failed                     */
+    BT_ERR_DEVICE_MEMORY = 5, /* device allocation failed / over budget   */
+    BT_ERR_CUDA = 6,        /* CUDA runtime error                         */
+    BT_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up         */
+    BT_ERR_STATE = 8,       /* call out of order (e.g. no graph uploaded) */
+    BT_ERR_NO_DEVICE = 9,   /* no CUDA device / wrong architecture        */
+    BT_ERR_OVERFLOW = 10    /* a result does not fit its output type      */
+} bt_status;
+
+typedef struct bt_graph bt_graph; /* host CSR, reference layout */
+typedef struct bt_ctx bt_ctx;     /* device context              */
+
+/* Read-only view of a host graph's arrays (owned by the bt_graph). */
+typedef struct {
+    uint32_t u_num, l_num, u_max, n;
+    uint64_t m;
+    uint64_t support_max;       /* set by bt_ebfc / the .bin header */
+    const uint32_t *offsets;    /* n+1 */
+    const uint32_t *neighbors;  /* 2m  */
+    const uint32_t *degrees;    /* n   */
+    const uint32_t *edges;      /* 2m  */
+    const uint32_t *edge_ids;   /* 2m  */
+} bt_graph_view;
+
+/* ---- host graph (replaces class Graph, src/graph/graph.h:30-52) ---------- */
+
+/* Graph(filename, false) + load_graph_bin: src/graph/graph.cpp:261-277,335-375.
+ * Unlike the reference it validates the header against the file size. */
+bt_status bt_graph_load_bin(const char *path, bt_graph **out);
+
+/* Graph(filename, true) / process_graph: src/graph/graph.cpp:74-242.
+ * Parses "u v" lines (first two integers of each line; lines starting with
+ * '%' and blank lines are skipped); ids must be < 99,999,999 (MAX_IDS,
+ * src/util/config.h:6). */
+bt_status bt_graph_load_text(const char *path, bt_graph **out);
+
+/* process_graph on an in-memory edge list in file order (same numbering). */
+bt_status bt_graph_from_edges(const uint32_t *u, const uint32_t *v, uint64_t m,
+                              bt_graph **out);
+
+/* graph_to_bin: src/graph/graph.cpp:293-318 (byte-identical output). */
+bt_status bt_graph_save_bin(const bt_graph *g, const char *path);
+
+bt_status bt_graph_get_view(const bt_graph *g, bt_graph_view *out);
+void bt_graph_free(bt_graph *g);
+
+/* ---- device context --------------------------------------------------- */
+
+/* Select `device`, create a stream and an empty context.  Fails with
+ * BT_ERR_NO_DEVICE when the device is absent or not sm_103. */
+bt_status bt_ctx_create(int device, bt_ctx **out);
+
+/* Run subsequent work on a caller-owned stream (cudaStream_t as void*);
+ * NULL restores the context's own stream. */
+bt_status bt_ctx_set_stream(bt_ctx *ctx, void *cuda_stream);
+
+/* Upper bound on device bytes this context may hold (0 = no limit).
+ * Allocations beyond it fail with BT_ERR_DEVICE_MEMORY. */
+bt_status bt_ctx_set_memory_budget(bt_ctx *ctx, uint64_t bytes);
+bt_status bt_ctx_memory_used(const bt_ctx *ctx, uint64_t *bytes);
+
+void bt_ctx_free(bt_ctx *ctx);
+
+/* Copy a host graph into the context's device arena (H2D of the reference
+ * CSR) and build the device layout: vertices relabelled by priority rank
+ * (degree, id) and rows sorted by rank.  Replaces the per-call cudaMalloc +
+ * cudaMemcpy of bfc_vpp.cu:245-267 and bitruss_msp.cu:453-465; the graph
+ * stays resident until the next upload or bt_ctx_free. */
+bt_status bt_graph_upload(bt_ctx *ctx, const bt_graph *g);
+
+/* ---- algorithms (on the resident graph) ------------------------------- */
+
+/* Global butterfly count.  Replaces bfc_vpp(Graph*): bfc_vpp.cu:321-385. */
+bt_status bt_bfc(bt_ctx *ctx, uint64_t *count);
+
+/* Per-edge butterfly support.  Replaces bfc_evpp(Graph*): bfc_vpp.cu:233-309.
+ * sup: m entries, by reference edge id (NULL: keep on device only).
+ * count / support_max may be NULL. */
+bt_status bt_ebfc(bt_ctx *ctx, uint64_t *sup, uint64_t *count, uint64_t *support_max);
+
+/* h-index bitruss numbers (true bitruss).  Replaces g_bitruss_hindex(Graph*):
+ * bitruss_hidx.cu:179-256.  bitruss: m entries (NULL: device only);
+ * rounds may be NULL. */
+bt_status bt_hidx(bt_ctx *ctx, uint32_t *bitruss, uint32_t *rounds);
+
+/* Multi-stage peeling (GBiD).  Replaces bitruss_msp(Graph*):
+ * bitruss_msp.cu:440-583, bit-exact with the reference's peel rule
+ * (bitruss_msp.cu:126-184).  levels: the reference's "bitruss msp with N
+ * levels" figure.  bitruss / levels may be NULL. */
+bt_status bt_msp(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels);
+
+/* Peeling with the corrected one-survivor rule; equals bt_hidx.  No
+ * reference counterpart (the reference's msp over-estimates some edges). */
+bt_status bt_msp_exact(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels);
+
+/* Copy the last per-edge result of this context (uint64 supports after
+ * bt_ebfc, uint32 bitruss after bt_hidx / bt_msp) to host memory. */
+bt_status bt_result_download(bt_ctx *ctx, void *host, size_t bytes);
+
+/* Device time in milliseconds of the named phase of the last call
+ * ("upload", "ebfc" (counting kernel), "peel" (peeling kernel), "msp" (peeling
+ * set-up + kernel + result), "hidx", "total"); negative if unknown. */
+double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
+
+/* Counters of the last msp/hidx call: [0] levels, [1] sub-rounds,
+ * [2] compressions, [3] peel tasks, [4] hidx rounds, [5] non-empty levels,
+ * [6] bucket splits; msp work: [8] pivot slots walked, [9] neighbour slots
+ * probed, [10] anchor slots, [11] butterflies found, [12] decrements, [13] m. */
+bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n);
+
+/* ---- errors ---------------------------------------------------------- */
+
+const char *bt_status_string(bt_status s);
+/* Message of the last failed call on this host thread ("" if none). */
+const char *bt_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BITRUSS_GB300_H */
