@@ -230,7 +230,7 @@ def run_ours(args):
         total_ms += e0.elapsed_time(e1)
         peel_ms.append(ctx.phase_ms("peel"))
         st = ctx.stats()
-        work = st[8:14]
+        work = st[8:17]
         launches += 5  # k_count, k_msp_init, k_two_hop, k_msp, k_msp_result
     torch.cuda.synchronize()
     barrier()
@@ -258,7 +258,7 @@ def run_ours(args):
 
     # roofline of k_msp
     mids, probes, anchor, hits, decs = work[:5]
-    alg_bytes = 8 * mids + 4 * probes + 4 * anchor + 8 * hits + 8 * decs
+    alg_bytes = 4 * probes + 4 * anchor + 8 * hits + 8 * decs
     t_peel = statistics.median(peel_ms) / 1000.0
     achieved = alg_bytes / t_peel / 1e9
     peak, peak_kind = load_peaks()
@@ -273,7 +273,9 @@ def run_ours(args):
                    "m": m, "n": int(g.n), "graph_digest": dig, "parallelism": "replicas",
                    "l2": "512 MB flush between timed steps; graph arrays > L2",
                    "levels": stats[0], "subrounds": stats[1], "tasks": stats[3],
-                   "peel_ms": statistics.median(peel_ms), "ebfc_ms": ctx.phase_ms("ebfc")},
+                   "peel_ms": statistics.median(peel_ms), "ebfc_ms": ctx.phase_ms("ebfc"),
+                   "kernel_phase_ms": {"level_transitions": work[6] / 1e6, "peel": work[7] / 1e6,
+                                       "finalize": work[8] / 1e6}},
         "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(4 * m)},
         "gpu_launches": launches,
@@ -281,7 +283,7 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "k_msp",
                      "algorithmic_bytes": int(alg_bytes),
-                     "work": {"pivot_slots": mids, "probes": probes, "anchor_slots": anchor,
+                     "work": {"tasks": mids, "probes": probes, "anchor_slots": anchor,
                               "butterflies": hits, "decrements": decs}},
         "clocks": clk,
     }
@@ -306,7 +308,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cl20m", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="cl20m",
+                    help="cl20m (default), er, or a scaled Chung-Lu case cl<k>k")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -259,10 +259,11 @@ class Context:
 
     def stats(self) -> list[int]:
         """[levels, sub-rounds, compressions, tasks, hidx rounds, non-empty
-        levels, bucket splits, -, pivot slots, probes, anchor slots,
-        butterflies found, decrements, m, -, -]"""
-        a = (C.c_uint64 * 16)()
-        _check(load().bt_ctx_stats(self._c, a, 16), "stats")
+        levels, bucket splits, -, peel tasks run, probes, anchor slots,
+        butterflies found, decrements, m, ns in level transitions, ns in
+        peel phases, ns in finalize phases, -, -, -]"""
+        a = (C.c_uint64 * 20)()
+        _check(load().bt_ctx_stats(self._c, a, 20), "stats")
         return list(a)
 
     def close(self):

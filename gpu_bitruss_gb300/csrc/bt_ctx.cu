@@ -11,6 +11,7 @@
 #include <mutex>
 #include <string>
 
+#include "bt_device.cuh"
 #include "bt_internal.h"
 
 // ---------------------------------------------------------------------------
@@ -108,6 +109,9 @@ void ctx_release_graph(bt_ctx *ctx) {
     ctx_free(ctx, g.eid0);
     ctx_free(ctx, g.ends);
     ctx_free(ctx, g.is_u);
+    ctx_free(ctx, g.hub_base);
+    ctx_free(ctx, g.hub_mask);
+    ctx_free(ctx, g.hub_pool);
     ctx_free(ctx, ctx->sup);
     ctx_free(ctx, ctx->result);
     ctx->sup = nullptr;
@@ -192,7 +196,7 @@ extern "C" double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase) {
 extern "C" bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n) {
     if (!ctx || !out) return bt_fail(BT_ERR_INVALID, "null argument");
     for (int i = 0; i < n && i < 8; i++) out[i] = ctx->stats[i];
-    for (int i = 8; i < n && i < 16; i++) out[i] = ctx->work[i - 8];
+    for (int i = 8; i < n && i < 20; i++) out[i] = ctx->work[i - 8];
     return BT_OK;
 }
 
@@ -238,6 +242,21 @@ __global__ void k_rows_relabel(uint32_t n, uint32_t u_num, const uint32_t *off, 
         }
     }
 }
+
+// hub table size of each row longer than the kernels' shared hash
+__global__ void k_hub_sizes(uint32_t n, const uint32_t *deg, uint32_t *size, uint32_t *mask) {
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
+        uint32_t sz = 0;
+        if (deg[x] > bt::kHashMaxDeg) {
+            sz = 64;
+            while (sz < 2 * deg[x]) sz <<= 1;
+        }
+        size[x] = sz;
+        mask[x] = sz ? sz - 1 : 0;
+    }
+}
+
+__global__ void k_hub_build(bt::Rows r, uint32_t n, uint2 *pool) { bt::hub_build(r, n, pool); }
 
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap) {
     uint64_t g = (n + block - 1) / block;
@@ -351,6 +370,34 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
     if (m) {
         STEPC(cub::DeviceSegmentedSort::SortPairs(temp, t3, t_nbr, g.nbr0, t_eid, g.eid0, (int64_t)(2 * m),
                                                   (int64_t)n, g.off, g.off + 1, st));
+    }
+    // hub tables
+    STEP(ctx_alloc_t(ctx, &g.hub_base, n ? n : 1));
+    STEP(ctx_alloc_t(ctx, &g.hub_mask, n ? n : 1));
+    if (n) {
+        k_hub_sizes<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.deg0, order, g.hub_mask);
+        STEPC(cudaGetLastError());
+        size_t t4 = 0;
+        STEPC(cub::DeviceScan::ExclusiveSum(nullptr, t4, order, g.hub_base, (int)n, st));
+        if (t4 > tb) {
+            ctx_free(ctx, temp);
+            temp = nullptr;
+            STEP(ctx_alloc(ctx, &temp, t4));
+            tb = t4;
+        }
+        STEPC(cub::DeviceScan::ExclusiveSum(temp, t4, order, g.hub_base, (int)n, st));
+        uint32_t last_base = 0, last_size = 0;
+        STEPC(cudaMemcpyAsync(&last_base, g.hub_base + n - 1, 4, cudaMemcpyDeviceToHost, st));
+        STEPC(cudaMemcpyAsync(&last_size, order + n - 1, 4, cudaMemcpyDeviceToHost, st));
+        STEPC(cudaStreamSynchronize(st));
+        g.hub_slots = (uint64_t)last_base + last_size;
+    }
+    STEP(ctx_alloc_t(ctx, &g.hub_pool, g.hub_slots ? g.hub_slots : 1));
+    if (g.hub_slots) {
+        STEPC(cudaMemsetAsync(g.hub_pool, 0xff, 8 * g.hub_slots, st));
+        bt::Rows rows{g.off, g.deg0, g.nbr0, g.eid0, g.hub_base, g.hub_mask, g.hub_pool};
+        k_hub_build<<<(unsigned)ctx->sm_count * 4, 256, 0, st>>>(rows, n, g.hub_pool);
+        STEPC(cudaGetLastError());
     }
     STEPC(cudaStreamSynchronize(st));
     cleanup();

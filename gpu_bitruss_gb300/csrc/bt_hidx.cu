@@ -34,7 +34,8 @@ constexpr uint32_t kEdgeChunk = 8;  // consecutive edge ids per grab (they share
 struct HidxArgs {
     bt::Rows rows;
     const uint2 *ends;
-    const uint32_t *two_hop;
+    const uint32_t *two_hop;   // per vertex: row probe total
+    const uint32_t *rowpre;    // per slot: prefix of the row's neighbour degrees
     const unsigned long long *prev;
     unsigned long long *curr;
     uint64_t m;
@@ -81,7 +82,8 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
     HSmem &sm = *reinterpret_cast<HSmem *>(smem_raw);
     bt::walk_init(sm.walk);
     const unsigned long long *prev = a.prev;
-    auto no_skip = [](uint32_t) { return false; };
+    auto keep_all = [](uint32_t, uint32_t) { return true; };
+    auto no_slice = [](uint32_t) {};
     bool any_change = false;
     for (;;) {
         if (threadIdx.x == 0) sm.e0 = atomicAdd(a.next_edge, (unsigned long long)kEdgeChunk);
@@ -98,20 +100,21 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
             const uint2 uv = a.ends[e];
             const uint32_t cu = a.two_hop[uv.x], cv = a.two_hop[uv.y];
             const uint32_t piv = cv <= cu ? uv.y : uv.x, anc = cv <= cu ? uv.x : uv.y;
-            bt::walk_stage(a.rows, sm.walk, anc);
-            const uint32_t pd = a.rows.deg[piv];
+            const uint32_t total = a.two_hop[piv];
             // pass 1: K = list length, cge = values >= H
             unsigned long long K = 0, cge = 0;
-            bt::walk_edge(a.rows, sm.walk, piv, anc, 0, pd, no_skip,
-                          [&](bool, bool valid, uint32_t e_pm, uint32_t e_my, uint32_t e_ay) {
-                              if (!valid) return;
-                              const unsigned long long p1 = prev[e_pm], p2 = prev[e_my], p3 = prev[e_ay];
-                              if (p1 == 0 || p2 == 0 || p3 == 0) return;
-                              unsigned long long v = p1 < p2 ? p1 : p2;
-                              v = v < p3 ? v : p3;
-                              K++;
-                              if (v >= H) cge++;
-                          });
+            bt::Walk &w = sm.walk;
+            bt::walk_range(a.rows, a.rowpre, w, piv, anc, total, 0, total, keep_all,
+                           [&](uint32_t k, uint32_t pos, uint32_t ah) {
+                               const unsigned long long p1 = prev[w.mid_eid[k]], p2 = prev[a.rows.eid[pos]],
+                                                        p3 = prev[bt::walk_anchor_edge(w, ah)];
+                               if (p1 == 0 || p2 == 0 || p3 == 0) return;
+                               unsigned long long v = p1 < p2 ? p1 : p2;
+                               v = v < p3 ? v : p3;
+                               K++;
+                               if (v >= H) cge++;
+                           },
+                           no_slice);
             block_sum2(sm, K, cge);
             unsigned long long h;
             if (cge >= H) {
@@ -130,17 +133,18 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
                     for (uint32_t t = threadIdx.x; t < kBuckets; t += blockDim.x) sm.hist[t] = 0;
                     __syncthreads();
                     unsigned long long above = 0, unused = 0;
-                    bt::walk_edge(a.rows, sm.walk, piv, anc, 0, pd, no_skip,
-                                  [&](bool, bool valid, uint32_t e_pm, uint32_t e_my, uint32_t e_ay) {
-                                      if (!valid) return;
-                                      const unsigned long long p1 = prev[e_pm], p2 = prev[e_my],
-                                                               p3 = prev[e_ay];
-                                      if (p1 == 0 || p2 == 0 || p3 == 0) return;
-                                      unsigned long long v = p1 < p2 ? p1 : p2;
-                                      v = v < p3 ? v : p3;
-                                      if (v >= hi) above++;
-                                      else if (v >= lo) atomicAdd(&sm.hist[(v - lo) / width], 1u);
-                                  });
+                    bt::walk_range(a.rows, a.rowpre, w, piv, anc, total, 0, total, keep_all,
+                                   [&](uint32_t k, uint32_t pos, uint32_t ah) {
+                                       const unsigned long long p1 = prev[w.mid_eid[k]],
+                                                                p2 = prev[a.rows.eid[pos]],
+                                                                p3 = prev[bt::walk_anchor_edge(w, ah)];
+                                       if (p1 == 0 || p2 == 0 || p3 == 0) return;
+                                       unsigned long long v = p1 < p2 ? p1 : p2;
+                                       v = v < p3 ? v : p3;
+                                       if (v >= hi) above++;
+                                       else if (v >= lo) atomicAdd(&sm.hist[(v - lo) / width], 1u);
+                                   },
+                                   no_slice);
                     block_sum2(sm, above, unused);
                     if (threadIdx.x == 0) {
                         // largest bucket b with count(values >= start_b) >= start_b
@@ -181,17 +185,8 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
     if (threadIdx.x == 0 && any_change) atomicExch(a.changed, 1u);
 }
 
-__global__ void k_two_hop_full(bt::Rows r, uint32_t n, uint32_t *out) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t x = warp; x < n; x += nw) {
-        const uint32_t b = r.off[x], d = r.deg[x];
-        unsigned long long s = 0;
-        for (uint32_t j = lane; j < d; j += 32) s += r.deg[r.nbr[b + j]];
-        s = warp_sum(s);
-        if (lane == 0) out[x] = s > 0xffffffffull ? 0xffffffffu : (uint32_t)s;
-    }
+__global__ void k_row_prefix(bt::Rows r, uint32_t n, uint32_t *rowpre, uint32_t *total) {
+    bt::row_prefix(r, n, rowpre, total);
 }
 
 __global__ void k_hidx_result(uint64_t m, const unsigned long long *v, uint32_t *out, unsigned *overflow) {
@@ -213,18 +208,20 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     cudaEvent_t e0 = ctx->ev[2], e1 = ctx->ev[3];
     cudaEventRecord(e0, st);
     unsigned long long *buf_a = nullptr, *buf_b = nullptr, *ctr = nullptr;
-    uint32_t *two_hop = nullptr;
+    uint32_t *two_hop = nullptr, *rowpre = nullptr;
     auto release = [&]() {
         ctx_free(ctx, buf_a);
         ctx_free(ctx, buf_b);
         ctx_free(ctx, ctr);
         ctx_free(ctx, two_hop);
+        ctx_free(ctx, rowpre);
     };
     bt_status rc;
     if ((rc = ctx_alloc_t(ctx, &buf_a, m ? m : 1)) != BT_OK ||
         (rc = ctx_alloc_t(ctx, &buf_b, m ? m : 1)) != BT_OK ||
         (rc = ctx_alloc_t(ctx, &ctr, 4)) != BT_OK ||
-        (rc = ctx_alloc_t(ctx, &two_hop, n ? n : 1)) != BT_OK) {
+        (rc = ctx_alloc_t(ctx, &two_hop, n ? n : 1)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &rowpre, m ? 2 * m : 1)) != BT_OK) {
         release();
         return rc;
     }
@@ -234,11 +231,11 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
         if (_e != cudaSuccess) { release(); return bt_cuda_fail(_e, #x, __FILE__, __LINE__); } \
     } while (0)
     C(cudaMemcpyAsync(buf_a, ctx->sup, 8 * m, cudaMemcpyDeviceToDevice, st));
-    bt::Rows rows{g.off, g.deg0, g.nbr0, g.eid0};
+    bt::Rows rows{g.off, g.deg0, g.nbr0, g.eid0, g.hub_base, g.hub_mask, g.hub_pool};
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (n) {
-        k_two_hop_full<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(rows, g.n,
-                                                                                                 two_hop);
+        k_row_prefix<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(
+            rows, g.n, rowpre, two_hop);
         C(cudaGetLastError());
     }
     const size_t smem = sizeof(HSmem);
@@ -252,7 +249,7 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     for (;;) {
         r++;
         C(cudaMemsetAsync(ctr, 0, 32, st));
-        HidxArgs a{rows, g.ends, two_hop, prev, curr, m, ctr, (unsigned *)(ctr + 1)};
+        HidxArgs a{rows, g.ends, two_hop, rowpre, prev, curr, m, ctr, (unsigned *)(ctr + 1)};
         if (m) {
             k_hidx_round<<<nblocks, kThreads, smem, st>>>(a);
             C(cudaGetLastError());
@@ -267,9 +264,11 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     }
     unsigned overflow = 0;
     C(cudaMemsetAsync(ctr + 2, 0, 4, st));
-    k_hidx_result<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
-        m, prev, ctx->result, (unsigned *)(ctr + 2));
-    C(cudaGetLastError());
+    if (m) {
+        k_hidx_result<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
+            m, prev, ctx->result, (unsigned *)(ctr + 2));
+        C(cudaGetLastError());
+    }
     C(cudaMemcpyAsync(&overflow, ctr + 2, 4, cudaMemcpyDeviceToHost, st));
     cudaEventRecord(e1, st);
     C(cudaStreamSynchronize(st));

@@ -65,6 +65,13 @@ struct DevGraph {
     uint32_t *eid0 = nullptr;   // 2m  reference edge id of each slot
     uint2 *ends = nullptr;      // m   (rank of U end, rank of V end) per edge id
     uint32_t *is_u = nullptr;   // n   1 if the rank's vertex is on the U side
+    // hub index: an open-addressing hash (neighbour rank -> edge id) of every
+    // row longer than the kernels' shared-memory hash; hub_mask[x] = table
+    // size - 1 (0: no table), hub_base[x] = first entry in hub_pool
+    uint32_t *hub_base = nullptr;
+    uint32_t *hub_mask = nullptr;
+    uint2 *hub_pool = nullptr;
+    uint64_t hub_slots = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -96,7 +103,7 @@ struct bt_ctx {
 
     double phase_ms[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
     uint64_t stats[8] = {0};
-    uint64_t work[8] = {0};  // msp work counters of the last call
+    uint64_t work[12] = {0};  // msp work counters and phase times of the last call
     cudaEvent_t ev[8] = {};
 };
 

@@ -46,7 +46,8 @@ namespace {
 using bt::kEmpty;
 using bt::kSliceMids;
 using bt::kThreads;
-constexpr uint32_t kTaskWork = 16384;      // target probes per task
+constexpr uint32_t kMinGrain = 512;         // probes per task, at least
+constexpr uint32_t kTasksPerCta = 2;        // target tasks per CTA per sub-round
 
 enum : uint8_t { ST_LIVE = 0, ST_CURR = 1, ST_DONE = 2 };
 
@@ -61,6 +62,7 @@ struct MspState {
     uint32_t len[2];               // frontier lists: len[par] = current, len[par^1] = next
     uint32_t near_len, near2_len, far_len, far2_len;
     uint32_t task_total, task_next, done;
+    unsigned long long ph_ns[4];   // CTA 0's time in: level transitions, peel, finalize
     // statistics
     unsigned long long subrounds, compressions, tasks, levels_seen, rebuilds;
     // work counters (algorithmic bytes): pivot slots walked, neighbour slots
@@ -80,12 +82,15 @@ struct MspArgs {
     const uint32_t *off;
     const uint2 *ends;
     uint32_t *deg, *nbr, *eid;      // live rows (compacted in place)
-    uint32_t *two_hop;              // per vertex: sum of live neighbour degrees
+    uint32_t *two_hop;              // per vertex: sum of live neighbour degrees (row probe total)
+    uint32_t *rowpre;               // per slot: prefix of the row's neighbour degrees
     unsigned long long *sup;        // working supports
     uint8_t *st;
     uint32_t *list_a, *list_b;      // curr / next (swap by parity)
     uint32_t *near_a, *near_b, *far_a, *far_b;
-    uint32_t *pl_piv, *pl_anc, *pl_ntask, *task_start;  // plan of the frontier
+    uint32_t *pl_piv, *pl_anc, *pl_grain, *task_start;  // plan of the frontier
+    const uint32_t *hub_base, *hub_mask;
+    const uint2 *hub_pool;
 };
 
 // ---------------------------------------------------------------------------
@@ -150,33 +155,48 @@ struct Smem {
     bt::Walk walk;
     uint32_t task, idx, k;
     uint32_t running;
+    unsigned long long total;
 };
 
-// Plan the frontier (one CTA): orientation and task count per edge, then the
-// prefix of task counts.
+// Plan the frontier (one CTA): orientation of every edge, then tasks of equal
+// probe counts.  The grain adapts to the sub-round's total work so that all
+// CTAs get tasks; an edge's grain is at least twice its anchor row (each task
+// stages that row).
 __device__ void plan_frontier(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t len) {
-    if (threadIdx.x == 0) sm.running = 0;
+    if (threadIdx.x == 0) {
+        sm.running = 0;
+        sm.total = 0;
+    }
     __syncthreads();
+    unsigned long long mine = 0;
+    for (uint32_t i = threadIdx.x; i < len; i += kThreads) {
+        const uint32_t e = curr[i];
+        const uint2 uv = a.ends[e];
+        const uint32_t cu = a.two_hop[uv.x], cv = a.two_hop[uv.y];
+        const uint32_t piv = cv <= cu ? uv.y : uv.x, anc = cv <= cu ? uv.x : uv.y;
+        a.pl_piv[i] = piv;
+        a.pl_anc[i] = anc;
+        mine += cv <= cu ? cv : cu;
+    }
+    for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+    if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&sm.total, mine);
+    __syncthreads();
+    unsigned long long g = sm.total / ((unsigned long long)kTasksPerCta * a.nblocks);
+    if (g < kMinGrain) g = kMinGrain;
+    if (g > (1u << 30)) g = 1u << 30;
+    unsigned long long anchor = 0;
     for (uint32_t base = 0; base < len; base += kThreads) {
-        uint32_t i = base + threadIdx.x;
+        const uint32_t i = base + threadIdx.x;
         uint32_t nt = 0;
         if (i < len) {
-            const uint32_t e = curr[i];
-            const uint2 uv = a.ends[e];
-            const uint32_t cu = a.two_hop[uv.x], cv = a.two_hop[uv.y];
-            uint32_t piv, anc, cost;
-            if (cv <= cu) { piv = uv.y; anc = uv.x; cost = cv; }
-            else { piv = uv.x; anc = uv.y; cost = cu; }
-            const uint32_t d = a.deg[piv];
-            nt = (d + kSliceMids - 1) / kSliceMids;
-            uint32_t byw = (cost + kTaskWork - 1) / kTaskWork;
-            if (byw > nt) nt = byw;
-            if (nt > d) nt = d;
-            if (nt == 0) nt = 1;
-            a.pl_piv[i] = piv;
-            a.pl_anc[i] = anc;
-            a.pl_ntask[i] = nt;
-            atomicAdd(&a.s->w_anchor, (unsigned long long)a.deg[anc]);
+            const uint32_t piv = a.pl_piv[i], anc = a.pl_anc[i];
+            const uint32_t work = a.two_hop[piv];
+            const uint32_t da = a.deg[anc];
+            unsigned long long gi = g > 2ull * da ? g : 2ull * da;
+            if (gi > (1u << 30)) gi = 1u << 30;
+            nt = (uint32_t)((work + gi - 1) / gi);
+            a.pl_grain[i] = (uint32_t)gi;
+            anchor += da;
         }
         uint32_t excl, tot;
         cub::BlockScan<uint32_t, kThreads>(sm.walk.scan).ExclusiveSum(nt, excl, tot);
@@ -185,6 +205,8 @@ __device__ void plan_frontier(const MspArgs &a, Smem &sm, const uint32_t *curr, 
         if (threadIdx.x == 0) sm.running += tot;
         __syncthreads();
     }
+    for (int o = 16; o; o >>= 1) anchor += __shfl_xor_sync(0xffffffffu, anchor, o);
+    if ((threadIdx.x & 31) == 0 && anchor) atomicAdd(&a.s->w_anchor, anchor);
     if (threadIdx.x == 0) {
         a.task_start[len] = sm.running;
         a.s->task_total = sm.running;
@@ -196,70 +218,84 @@ __device__ void plan_frontier(const MspArgs &a, Smem &sm, const uint32_t *curr, 
 __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t curr_len,
                            uint32_t *next, uint32_t *next_len, uint32_t *near_list,
                            unsigned long long L, unsigned long long hi, Work &wk) {
-    const uint32_t lane = threadIdx.x & 31;
-    const bt::Rows rows{a.off, a.deg, a.nbr, a.eid};
+    const bt::Rows rows{a.off, a.deg, a.nbr, a.eid, a.hub_base, a.hub_mask, a.hub_pool};
     const uint8_t *st = a.st;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const uint32_t t = atomicAdd(&a.s->task_next, 1u);
-            sm.task = t;
-            if (t < a.s->task_total) {
-                // frontier index: last i with task_start[i] <= t
-                uint32_t lo = 0, hi2 = curr_len;
-                while (hi2 - lo > 1) {
-                    const uint32_t md = (lo + hi2) >> 1;
-                    if (a.task_start[md] <= t) lo = md;
-                    else hi2 = md;
-                }
-                sm.idx = lo;
-                sm.k = t - a.task_start[lo];
+    const uint32_t ntasks = a.s->task_total;
+    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
+        // frontier edge of task t: last i with task_start[i] <= t
+        if (threadIdx.x < 32) {
+            const uint32_t i = bt::warp_find_slot(a.task_start, curr_len, t);
+            if (threadIdx.x == 0) {
+                sm.idx = i;
+                sm.k = t - a.task_start[i];
             }
         }
         __syncthreads();
-        if (sm.task >= a.s->task_total) break;
         const uint32_t i = sm.idx, k = sm.k;
         const uint32_t uv = curr[i];
-        const uint32_t piv = a.pl_piv[i], anc = a.pl_anc[i], nt = a.pl_ntask[i];
+        const uint32_t piv = a.pl_piv[i], anc = a.pl_anc[i], gi = a.pl_grain[i];
         const bool piv_is_v = (piv == a.ends[uv].y);
-        bt::walk_stage(rows, sm.walk, anc);
-        const uint32_t pd = a.deg[piv];
-        const uint32_t s0 = (uint32_t)(((unsigned long long)pd * k) / nt);
-        const uint32_t s1 = (uint32_t)(((unsigned long long)pd * (k + 1)) / nt);
+        const uint32_t total = a.two_hop[piv];
+        const uint32_t f0 = k * gi;
+        const uint32_t f1 = total - f0 < gi ? total : f0 + gi;
         const uint32_t exact = a.exact;
-        if (threadIdx.x == 0) wk.mids += s1 - s0;
-        bt::walk_edge(
-            rows, sm.walk, piv, anc, s0, s1, [&](uint32_t e_pm) { return st[e_pm] == ST_DONE; },
-            [&](bool active, bool valid, uint32_t e_pm, uint32_t e_my, uint32_t e_ay) {
-                uint32_t dec = 0;
-                wk.probes += active;
-                if (valid) {
-                    const uint8_t s_ay = st[e_ay], s_my = st[e_my];
-                    if (s_ay != ST_DONE && s_my != ST_DONE) {
-                        wk.hits++;
-                        const bool c_pm = st[e_pm] == ST_CURR;
-                        const bool c_my = s_my == ST_CURR, c_ay = s_ay == ST_CURR;
-                        // name the edges as the reference does: w on u's side, x on v's
-                        uint32_t wv, ux;
-                        bool cwv, cux;
-                        if (piv_is_v) { wv = e_pm; ux = e_ay; cwv = c_pm; cux = c_ay; }
-                        else { wv = e_ay; ux = e_pm; cwv = c_ay; cux = c_pm; }
-                        const uint32_t d = peel_rule(uv, wv, e_my, ux, cwv, c_my, cux, exact);
-                        // re-express as bits: 1 = e_pm, 2 = e_my, 4 = e_ay
-                        const uint32_t d_wv = d & 1, d_wx = (d >> 1) & 1, d_ux = (d >> 2) & 1;
-                        dec = piv_is_v ? (d_wv | (d_wx << 1) | (d_ux << 2))
-                                       : (d_ux | (d_wx << 1) | (d_wv << 2));
+        if (threadIdx.x == 0) wk.mids++;
+        bt::Walk &w = sm.walk;
+        bt::walk_range(
+            rows, a.rowpre, w, piv, anc, total, f0, f1,
+            [&](uint32_t k, uint32_t e_pm) {
+                const uint8_t sp = st[e_pm];
+                w.pm_curr[k] = sp == ST_CURR;
+                return sp != ST_DONE;
+            },
+            [&](uint32_t k, uint32_t pos, uint32_t ah) {
+                const uint32_t e_pm = w.mid_eid[k];
+                const uint32_t e_ay = bt::walk_anchor_edge(w, ah);
+                const uint32_t e_my = a.eid[pos];
+                const uint8_t s_ay = st[e_ay], s_my = st[e_my];
+                wk.hits++;
+                if (s_ay == ST_DONE || s_my == ST_DONE) return;
+                const bool c_pm = w.pm_curr[k], c_my = s_my == ST_CURR, c_ay = s_ay == ST_CURR;
+                // name the edges as the reference does: w on u's side, x on v's
+                uint32_t wv, ux;
+                bool cwv, cux;
+                if (piv_is_v) { wv = e_pm; ux = e_ay; cwv = c_pm; cux = c_ay; }
+                else { wv = e_ay; ux = e_pm; cwv = c_ay; cux = c_pm; }
+                const uint32_t d = peel_rule(uv, wv, e_my, ux, cwv, c_my, cux, exact);
+                if (!d) return;
+                const bool d_wv = d & 1, d_wx = d & 2, d_ux = d & 4;
+                const bool dec_pm = piv_is_v ? d_wv : d_ux;
+                const bool dec_ay = piv_is_v ? d_ux : d_wv;
+                wk.decs += (uint32_t)dec_pm + (uint32_t)d_wx + (uint32_t)dec_ay;
+                if (dec_pm) atomicAdd(&w.slot_dec[k], 1u);
+                if (d_wx) dec_edge(a, next, next_len, near_list, L, hi, e_my, 1);
+                if (dec_ay) {
+                    if (w.cached_size) atomicAdd(&w.hdec[ah], 1u);
+                    else dec_edge(a, next, next_len, near_list, L, hi, e_ay, 1);
+                }
+            },
+            [&](uint32_t cl) {
+                __syncthreads();
+                if (threadIdx.x < cl) {
+                    const uint32_t c = w.slot_dec[threadIdx.x];
+                    if (c) {
+                        w.slot_dec[threadIdx.x] = 0;
+                        dec_edge(a, next, next_len, near_list, L, hi, w.mid_eid[threadIdx.x], c);
                     }
                 }
-                // e_pm is shared by the lanes probing the same mid: aggregate
-                const bool want = dec & 1;
-                const uint32_t key = want ? e_pm : (0x80000000u | lane);
-                const uint32_t grp = __match_any_sync(0xffffffffu, key);
-                wk.decs += __popc(dec);
-                if (want && lane == (uint32_t)(__ffs(grp) - 1))
-                    dec_edge(a, next, next_len, near_list, L, hi, e_pm, __popc(grp));
-                if (dec & 2) dec_edge(a, next, next_len, near_list, L, hi, e_my, 1);
-                if (dec & 4) dec_edge(a, next, next_len, near_list, L, hi, e_ay, 1);
             });
+        // flush the anchor-side decrements of this task
+        if (w.cached_size) {
+            for (uint32_t h = threadIdx.x; h < w.cached_size; h += kThreads) {
+                const uint32_t c = w.hdec[h];
+                if (c) {
+                    w.hdec[h] = 0;
+                    dec_edge(a, next, next_len, near_list, L, hi, w.hval[h], c);
+                }
+            }
+        }
+        if (threadIdx.x == 0) wk.probes += f1 - f0;
+        __syncthreads();
     }
     __syncthreads();
 }
@@ -312,23 +348,15 @@ __device__ void compress_rows(const MspArgs &a) {
 }
 
 __device__ void compute_two_hop(const MspArgs &a) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t x = warp; x < a.n; x += nw) {
-        const uint32_t b = a.off[x], d = a.deg[x];
-        unsigned long long s = 0;
-        for (uint32_t j = lane; j < d; j += 32) s += a.deg[a.nbr[b + j]];
-        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) a.two_hop[x] = s > 0xffffffffull ? 0xffffffffu : (uint32_t)s;
-    }
+    const bt::Rows rows{a.off, a.deg, a.nbr, a.eid, a.hub_base, a.hub_mask, a.hub_pool};
+    bt::row_prefix(rows, a.n, a.rowpre, a.two_hop);
 }
 
 // ---------------------------------------------------------------------------
 // the persistent kernel
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads) k_msp(MspArgs a) {
+__global__ void __launch_bounds__(kThreads, 2) k_msp(MspArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
     MspState *s = a.s;
@@ -340,6 +368,14 @@ __global__ void __launch_bounds__(kThreads) k_msp(MspArgs a) {
     uint32_t par = 0;  // lists[par] is the frontier, lists[par ^ 1] the next frontier
     if (gtid == 0) s->min_sup = ~0ull;
     if (!barrier(a)) return;
+    unsigned long long t_mark = gtid == 0 ? bt::global_ns() : 0;
+    auto lap = [&](int k) {
+        if (gtid == 0) {
+            const unsigned long long t = bt::global_ns();
+            s->ph_ns[k] += t - t_mark;
+            t_mark = t;
+        }
+    };
 
     for (;;) {
         // ------------------------------------------------ level transition
@@ -419,6 +455,7 @@ __global__ void __launch_bounds__(kThreads) k_msp(MspArgs a) {
                 }
             }
             if (!barrier(a)) return;
+            lap(0);
         }
         // ------------------------------------------------ sub-round
         const unsigned long long L = s->level, hi = s->hi;
@@ -426,6 +463,7 @@ __global__ void __launch_bounds__(kThreads) k_msp(MspArgs a) {
         uint32_t *curr = lists[par], *next = lists[par ^ 1];
         peel_tasks(a, sm, curr, curr_len, next, &s->len[par ^ 1], a.near_a, L, hi, wk);
         if (!barrier(a)) return;
+        lap(1);
         // finalize: frontier -> processed, next -> frontier (clamped at L)
         const uint32_t next_len = s->len[par ^ 1];
         for (uint32_t i = gtid; i < curr_len; i += gsz) a.st[curr[i]] = ST_DONE;
@@ -445,6 +483,7 @@ __global__ void __launch_bounds__(kThreads) k_msp(MspArgs a) {
         if (blockIdx.x == 0 && next_len) plan_frontier(a, sm, next, next_len);
         par ^= 1;
         if (!barrier(a)) return;
+        lap(2);
     }
     if (gtid == 0) s->done = 1;
     // flush the work counters (one atomic per warp)
@@ -546,7 +585,8 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     A(a.far_b, 4 * mm);
     A(a.pl_piv, 4 * mm);
     A(a.pl_anc, 4 * mm);
-    A(a.pl_ntask, 4 * mm);
+    A(a.pl_grain, 4 * mm);
+    A(a.rowpre, 8 * mm);
     A(a.task_start, 4 * (mm + 1));
 #undef A
 #define C(x)                                                                  \
@@ -575,6 +615,9 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     a.wait_ns = wait_limit_ns();
     a.off = g.off;
     a.ends = g.ends;
+    a.hub_base = g.hub_base;
+    a.hub_mask = g.hub_mask;
+    a.hub_pool = g.hub_pool;
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (m) {
         k_msp_init<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
@@ -639,6 +682,9 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     ctx->work[3] = h.w_hits;
     ctx->work[4] = h.w_decs;
     ctx->work[5] = m;
+    ctx->work[6] = h.ph_ns[0];
+    ctx->work[7] = h.ph_ns[1];
+    ctx->work[8] = h.ph_ns[2];
     ctx->last_result = 2;
     if (levels) *levels = (uint32_t)h.last_level;
     return BT_OK;

@@ -141,8 +141,10 @@ double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
 
 /* Counters of the last msp/hidx call: [0] levels, [1] sub-rounds,
  * [2] compressions, [3] peel tasks, [4] hidx rounds, [5] non-empty levels,
- * [6] bucket splits; msp work: [8] pivot slots walked, [9] neighbour slots
- * probed, [10] anchor slots, [11] butterflies found, [12] decrements, [13] m. */
+ * [6] bucket splits; msp work: [8] peel tasks run, [9] neighbour slots
+ * probed, [10] anchor slots, [11] butterflies found, [12] decrements, [13] m;
+ * [14..16] nanoseconds the peeling kernel spent in level transitions, peel
+ * phases and finalize phases. */
 bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n);
 
 /* ---- errors ---------------------------------------------------------- */
