@@ -26,7 +26,7 @@ import numpy as np
 
 __all__ = [
     "BitrussError", "Graph", "Context", "load", "build",
-    "bfc_vpp", "bfc_evpp", "g_bitruss_hindex", "bitruss_msp", "bitruss_msp_exact",
+    "bfc_vpp", "bfc_evpp", "g_bitruss_hindex", "bitruss_msp", "bitruss_msp_exact", "bfc_noalloc",
     "STATUS", "SYMBOLS",
 ]
 
@@ -47,6 +47,7 @@ SYMBOLS = [
     "bt_ctx_set_memory_budget", "bt_ctx_memory_used", "bt_ctx_free", "bt_graph_upload",
     "bt_bfc", "bt_ebfc", "bt_hidx", "bt_msp", "bt_msp_exact", "bt_result_download",
     "bt_ctx_phase_ms", "bt_ctx_stats", "bt_status_string", "bt_last_error",
+    "bt_bfc_noalloc",
 ]
 
 
@@ -107,6 +108,7 @@ def load():
         "bt_ctx_stats": ([P, C.POINTER(u64), i32], i32),
         "bt_status_string": ([i32], C.c_char_p),
         "bt_last_error": ([], C.c_char_p),
+        "bt_bfc_noalloc": ([i32, P, P, u32, u64, P, P], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -315,6 +317,14 @@ def bitruss_msp(g: Graph) -> np.ndarray:
     b, lv = _ctx_for(g).msp()
     g.bitruss, g.levels = b, lv
     return b
+
+
+def bfc_noalloc(device: int, d_offsets: int, d_neighbors: int, n: int, m: int,
+                d_count: int, stream: int = 0) -> None:
+    """Butterfly count into caller-owned device buffers (raw device pointers),
+    without any device allocation by the library; enqueued on `stream`."""
+    _check(load().bt_bfc_noalloc(device, C.c_void_p(d_offsets), C.c_void_p(d_neighbors), n, m,
+                                 C.c_void_p(d_count), C.c_void_p(stream or 0)), "bt_bfc_noalloc")
 
 
 def bitruss_msp_exact(g: Graph) -> np.ndarray:

@@ -20,7 +20,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libbitruss.so")
 COH = os.path.join(PKG, "coh")
 
-CUDA_SOURCES = ["bt_ctx.cu", "bt_count.cu", "bt_msp.cu", "bt_hidx.cu"]
+CUDA_SOURCES = ["bt_ctx.cu", "bt_count.cu", "bt_msp.cu", "bt_hidx.cu", "bt_noalloc.cu"]
 CXX_SOURCES = ["bt_graph.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 

@@ -147,6 +147,26 @@ double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
  * phases and finalize phases. */
 bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n);
 
+/* ---- allocation-free variant ------------------------------------------ */
+
+/* Global butterfly count that allocates no device memory.  No counterpart in
+ * the reference.  For callers that may not allocate on the device -- plugin
+ * hosts that own the device heap and only hand buffers in, or
+ * latency-sensitive paths that cannot afford a cudaMalloc / cudaFree -- the
+ * caller passes the graph and the output in its own device buffers:
+ * d_offsets (n+1) and d_neighbors (2m) in the reference layout (Graph::offsets
+ * and Graph::neighbors copied to the device), d_count one uint64 that receives
+ * the count.  Work is enqueued on `stream` (cudaStream_t as void*, NULL =
+ * default stream); the count is ready when the stream reaches that point.
+ * Scratch is one 32 MiB device array inside the library, held by every GPU
+ * that loads it until the process exits; graphs with more than 4,194,304
+ * vertices are rejected with BT_ERR_INVALID.  The first call on a device looks
+ * up that array's device address (once per device) and should come before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and give wrong counts. */
+bt_status bt_bfc_noalloc(int device, const uint32_t *d_offsets, const uint32_t *d_neighbors,
+                         uint32_t n, uint64_t m, unsigned long long *d_count, void *stream);
+
 /* ---- errors ---------------------------------------------------------- */
 
 const char *bt_status_string(bt_status s);
