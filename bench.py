@@ -275,7 +275,10 @@ def run_ours(args):
                    "levels": stats[0], "subrounds": stats[1], "tasks": stats[3],
                    "peel_ms": statistics.median(peel_ms), "ebfc_ms": ctx.phase_ms("ebfc"),
                    "kernel_phase_ms": {"level_transitions": work[6] / 1e6, "peel": work[7] / 1e6,
-                                       "finalize": work[8] / 1e6}},
+                                       "finalize": work[8] / 1e6},
+                   "cta_ms_by_step": dict(zip(["task", "stage", "slice", "probe", "hits", "flush",
+                                               "barrier", "other"],
+                                              [round(c / 2.07e6, 1) for c in stats[20:28]]))},
         "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(4 * m)},
         "gpu_launches": launches,

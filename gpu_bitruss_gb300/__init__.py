@@ -263,9 +263,11 @@ class Context:
         """[levels, sub-rounds, compressions, tasks, hidx rounds, non-empty
         levels, bucket splits, -, peel tasks run, probes, anchor slots,
         butterflies found, decrements, m, ns in level transitions, ns in
-        peel phases, ns in finalize phases, -, -, -]"""
-        a = (C.c_uint64 * 20)()
-        _check(load().bt_ctx_stats(self._c, a, 20), "stats")
+        peel phases, ns in finalize phases, -, -, -, then SM cycles per CTA
+        of the peeling kernel by step: task, stage, slice, probe, hits, flush,
+        barrier, other]"""
+        a = (C.c_uint64 * 28)()
+        _check(load().bt_ctx_stats(self._c, a, 28), "stats")
         return list(a)
 
     def close(self):

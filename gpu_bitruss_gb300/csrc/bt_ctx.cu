@@ -197,6 +197,7 @@ extern "C" bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n) {
     if (!ctx || !out) return bt_fail(BT_ERR_INVALID, "null argument");
     for (int i = 0; i < n && i < 8; i++) out[i] = ctx->stats[i];
     for (int i = 8; i < n && i < 20; i++) out[i] = ctx->work[i - 8];
+    for (int i = 20; i < n && i < 28; i++) out[i] = ctx->prof[i - 20];
     return BT_OK;
 }
 
@@ -247,7 +248,7 @@ __global__ void k_rows_relabel(uint32_t n, uint32_t u_num, const uint32_t *off, 
 __global__ void k_hub_sizes(uint32_t n, const uint32_t *deg, uint32_t *size, uint32_t *mask) {
     for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n; x += gridDim.x * blockDim.x) {
         uint32_t sz = 0;
-        if (deg[x] > bt::kHashMaxDeg) {
+        if (deg[x] > bt::kHubMinDeg) {
             sz = 64;
             while (sz < 2 * deg[x]) sz <<= 1;
         }

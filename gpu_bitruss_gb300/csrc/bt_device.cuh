@@ -12,6 +12,7 @@ namespace bt {
 constexpr int kThreads = 512;
 constexpr int kHashSlots = 4096;            // shared-memory hash capacity (slots)
 constexpr uint32_t kHashMaxDeg = kHashSlots / 2;
+constexpr uint32_t kHubMinDeg = 256;        // rows longer than this get a global hub table
 constexpr uint32_t kSliceMids = kThreads;   // mids per slice (one block scan)
 constexpr uint32_t kPerThread = 4;          // consecutive probes per thread per round
 constexpr uint32_t kRound = kThreads * kPerThread;
@@ -99,27 +100,51 @@ struct Rows {
 
 struct Walk {
     // anchor row staged as a hash: vertex -> edge id, plus a pending
-    // decrement count per entry (peeling)
+    // decrement count per entry (peeling); arow / aslot list the row in order
+    // with each entry's hash slot
     uint32_t hkey[kHashSlots];
     uint32_t hval[kHashSlots];
     uint32_t hdec[kHashSlots];
+    uint32_t arow[kHashMaxDeg];
+    uint16_t aslot[kHashMaxDeg];
     // one slice of at most kSliceMids pivot slots
     uint32_t mid_eid[kSliceMids];
-    uint32_t mid_base[kSliceMids];
-    uint32_t pre[kSliceMids + 1];
+    uint32_t mid_base[kSliceMids];   // forward: mid's row start; reverse: its hub table
+    uint32_t mid_mask[kSliceMids];   // 0: forward (walk mid's row); else reverse (hub mask)
+    uint32_t mid_j0[kSliceMids];     // first position walked in the row
+    uint32_t pre[kSliceMids + 1];    // prefix of the positions walked per slot
     uint32_t slot_dec[kSliceMids];
-    uint8_t ok[kSliceMids];
     uint8_t pm_curr[kSliceMids];
     // butterflies found in the current round
-    uint16_t hit_k[kHitCap];
-    uint32_t hit_pos[kHitCap];
+    uint16_t hit_k[kHitCap];         // slot, | kRevHit when found walking anc's row
+    uint32_t hit_pos[kHitCap];       // edge id (mid, y)
     uint32_t hit_a[kHitCap];
     uint32_t hit_n[2];
     uint32_t cached_anc, cached_size;  // staged anchor; size 0: use its hub table
+    uint32_t cached_deg;               // length of arow
+    uint32_t cached_epoch;             // row-compaction epoch the anchor was staged in
     uint32_t gbase, gmask;             // hub table of the staged anchor
     uint32_t s_lo, s_hi;
+    // cycle counters of this CTA's thread 0 (see prof_mark)
+    unsigned long long prof_t, prof[8];
+    unsigned long long walked;         // row positions walked (forward + reverse)
     typename cub::BlockScan<uint32_t, kThreads>::TempStorage scan;
 };
+
+constexpr uint16_t kRevHit = 0x8000;
+
+// Per-CTA time accounting: thread 0 charges the SM cycles since the previous
+// mark to counter k.  Marks sit right after block-wide synchronisation, so
+// the counters split the CTA's time between the steps of the walk.
+enum { PF_TASK = 0, PF_STAGE = 1, PF_SLICE = 2, PF_PROBE = 3, PF_HITS = 4, PF_FLUSH = 5,
+       PF_BARRIER = 6, PF_OTHER = 7 };
+__device__ __forceinline__ void prof_mark(Walk &w, int k) {
+    if (threadIdx.x == 0) {
+        const unsigned long long t = clock64();
+        w.prof[k] += t - w.prof_t;
+        w.prof_t = t;
+    }
+}
 
 __device__ __forceinline__ uint32_t hash_slot(uint32_t y, uint32_t mask) {
     return (y * 0x9E3779B1u) & mask;
@@ -134,18 +159,23 @@ __device__ inline void walk_init(Walk &w) {
     if (threadIdx.x == 0) {
         w.cached_anc = kEmpty;
         w.cached_size = 0;
+        w.cached_epoch = 0;
         w.hit_n[0] = w.hit_n[1] = 0;
+        for (int k = 0; k < 8; k++) w.prof[k] = 0;
+        w.walked = 0;
+        w.prof_t = clock64();
     }
     __syncthreads();
 }
 
 // Stage anc's live row as a shared-memory hash vertex -> edge id (rows
-// longer than kHashMaxDeg use their global hub table instead).  Rows only ever
-// lose processed edges, so a table built earlier for the same vertex stays a
-// valid superset (callers check every edge's state).  Block-uniform; the
-// caller has synchronised since the last lookup.
-__device__ inline void walk_stage(const Rows &r, Walk &w, uint32_t anc) {
-    if (w.cached_anc == anc) {
+// longer than kHashMaxDeg use their global hub table instead).  `epoch`
+// counts row compactions: a staged row is reused only within one epoch, so
+// every CTA walks the same anchor row (the split of a slot's work between
+// tasks depends on its length).  Block-uniform; the caller has synchronised
+// since the last lookup.
+__device__ inline void walk_stage(const Rows &r, Walk &w, uint32_t anc, uint32_t epoch) {
+    if (w.cached_anc == anc && w.cached_epoch == epoch) {
         __syncthreads();
         return;
     }
@@ -168,16 +198,38 @@ __device__ inline void walk_stage(const Rows &r, Walk &w, uint32_t anc) {
                 }
                 h = (h + 1) & mask;
             }
+            w.arow[j] = y;
+            w.aslot[j] = (uint16_t)h;
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         w.cached_anc = anc;
+        w.cached_epoch = epoch;
         w.cached_size = size;
         w.gbase = size ? 0 : r.hub_base[anc];
         w.gmask = size ? 0 : r.hub_mask[anc];
+        w.cached_deg = d;
     }
     __syncthreads();
+}
+
+// Edge id (x, y) from x's hub table (base, mask), or kEmpty.
+__device__ __forceinline__ uint32_t hub_lookup(const uint2 *pool, uint32_t base, uint32_t mask, uint32_t y) {
+    // buckets of 4 (key, edge id) pairs, 32 bytes: one sector per probe
+    const uint4 *tab = reinterpret_cast<const uint4 *>(pool + base);
+    uint32_t b = hash_slot(y, mask) >> 2;
+    const uint32_t bmask = mask >> 2;
+    for (uint32_t probe = 0; probe <= bmask; probe++) {
+        const uint4 q0 = tab[2 * b], q1 = tab[2 * b + 1];
+        if (q0.x == y) return q0.y;
+        if (q0.z == y) return q0.w;
+        if (q1.x == y) return q1.y;
+        if (q1.z == y) return q1.w;
+        if (q0.x == kEmpty || q0.z == kEmpty || q1.x == kEmpty || q1.z == kEmpty) return kEmpty;
+        b = (b + 1) & bmask;
+    }
+    return kEmpty;
 }
 
 // Where y sits in the staged anchor: its shared hash slot when the anchor is
@@ -196,23 +248,14 @@ __device__ __forceinline__ uint32_t walk_lookup(const Rows &r, const Walk &w, ui
         }
         return kEmpty;
     }
-    const uint32_t mask = w.gmask;
-    const uint2 *tab = r.hub_pool + w.gbase;
-    uint32_t h = hash_slot(y, mask);
-    for (uint32_t probe = 0; probe <= mask; probe++) {
-        const uint2 kv = tab[h];
-        if (kv.x == y) return kv.y;
-        if (kv.x == kEmpty) return kEmpty;
-        h = (h + 1) & mask;
-    }
-    return kEmpty;
+    return hub_lookup(r.hub_pool, w.gbase, w.gmask, y);
 }
 
 __device__ __forceinline__ uint32_t walk_anchor_edge(const Walk &w, uint32_t a) {
     return w.cached_size ? w.hval[a] : a;
 }
 
-// Build the hub tables (one CTA per row longer than kHashMaxDeg).
+// Build the hub tables (one CTA per row longer than kHubMinDeg).
 __device__ inline void hub_build(const Rows &r, uint32_t n, uint2 *pool) {
     for (uint32_t x = blockIdx.x; x < n; x += gridDim.x) {
         const uint32_t mask = r.hub_mask[x];
@@ -220,7 +263,8 @@ __device__ inline void hub_build(const Rows &r, uint32_t n, uint2 *pool) {
         const uint32_t b = r.off[x], d = r.deg[x], base = r.hub_base[x];
         for (uint32_t j = threadIdx.x; j < d; j += blockDim.x) {
             const uint32_t y = r.nbr[b + j], e = r.eid[b + j];
-            uint32_t h = hash_slot(y, mask);
+            // linear probing from the start of the key's 4-slot bucket (see hub_lookup)
+            uint32_t h = hash_slot(y, mask) & ~3u;
             for (uint32_t probe = 0; probe <= mask; probe++) {
                 const uint32_t prev = atomicCAS(&pool[base + h].x, kEmpty, y);
                 if (prev == kEmpty || prev == y) {
@@ -253,59 +297,106 @@ __device__ inline uint32_t warp_find_slot(const uint32_t *pre, uint32_t d, uint3
 }
 
 // Walk the butterflies of one edge between pivot `piv` and anchor `anc`
-// over the probe range [f0, f1) of piv's row (anc is staged here).  The probe
-// space of a row is its mids' rows laid end to end: rowpre[pb + s] is the
-// exclusive prefix of the degrees of the row's mids (as of the last row
-// compaction) and `total` the row sum, so probe f is slot s (last with
-// rowpre <= f) at position f - rowpre[pb + s] of mid's row.
+// over the share [f0, f1) of piv's row (anc is staged here).  The shares are
+// cut in the plain probe space of the row -- its mids' rows laid end to end:
+// rowpre[pb + s] is the exclusive prefix of the degrees of the row's mids (as
+// of the last row compaction) and `total` the row sum -- so slot s owns
+// [rowpre[pb+s], rowpre[pb+s+1]) and a share covers parts of whole slots.
+//
+// Each (mid, anc) pair is intersected from the shorter side: forward, mid's
+// row is walked and each y looked up in anc's staged hash (or hub table);
+// reverse (mid has a hub table and a longer row than anc), anc's row is
+// walked and each y looked up in mid's hub table.  A slot's part of the share
+// maps onto the walked row proportionally, so the shares of a slot partition
+// that row exactly.
 //
 // Slices of at most kSliceMids pivot slots are loaded into shared memory;
-// prep_slot(k, e_pm) runs once per slot and says whether to probe its mid
-// (the walk itself skips mid == anc).  Each round then probes kRound slots
-// (kPerThread consecutive ones per thread) and queues the hits -- mids'
-// neighbours y != piv that are also in anc's row -- in shared memory, and a
-// second pass calls on_hit(k, pos, a) once per hit with all threads busy:
-// k = slice slot of mid, pos = index of (mid, y) in the row arrays,
-// a = walk_lookup's answer for y.  slice_done(cl) runs (block-uniform) after
-// each slice's last hit.
+// prep_slot(k, e_pm) runs once per slot and says whether to walk its mid
+// (the walk itself skips mid == anc).  Each round walks kRound positions
+// (kPerThread consecutive ones per thread) and queues the hits -- y != piv
+// adjacent to both mid and anc -- in shared memory; a second pass hands every
+// hit to on_hit with all threads busy, in two steps so that the memory
+// traffic of several hits overlaps: on_hit.load(state, k, e_my, a) (loads
+// only) for up to kPerThread hits, then on_hit.apply(state) for each.  k =
+// slice slot of mid (| kRevHit for a reverse hit), e_my = the edge id
+// (mid, y), a = the anchor's answer for y (walk_lookup's convention: a hash
+// slot when anc is staged, else the edge id).  slice_done(cl, last) runs
+// (block-uniform) after each slice's last hit; last marks the final slice.
 template <class PrepSlot, class OnHit, class SliceDone>
-__device__ inline void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w, uint32_t piv,
-                                  uint32_t anc, uint32_t total, uint32_t f0, uint32_t f1,
-                                  PrepSlot prep_slot, OnHit on_hit, SliceDone slice_done) {
+__device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w, uint32_t piv,
+                                           uint32_t anc, uint32_t epoch, uint32_t total, uint32_t f0,
+                                           uint32_t f1, PrepSlot prep_slot, OnHit &on_hit,
+                                           SliceDone slice_done) {
     if (f0 >= f1) return;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t pb = r.off[piv], pd = r.deg[piv];
     const uint32_t *pre = rowpre + pb;
-    if (warp == 0) {
-        const uint32_t t = warp_find_slot(pre, pd, f0);
-        if (lane == 0) w.s_lo = t;
-    } else if (warp == 1) {
-        const uint32_t t = warp_find_slot(pre, pd, f1 - 1);
-        if (lane == 0) w.s_hi = t;
-    }
-    walk_stage(r, w, anc);  // synchronises the block
-    const uint32_t s_lo = w.s_lo, s_hi = w.s_hi;
+    uint32_t s_lo = 0, s_hi = 0;
+    if (warp == 0) s_lo = warp_find_slot(pre, pd, f0);
+    else if (warp == 1) s_hi = warp_find_slot(pre, pd, f1 - 1);
+    walk_stage(r, w, anc, epoch);  // synchronises the block
+    prof_mark(w, PF_STAGE);
+    if (warp == 0 && lane == 0) w.s_lo = s_lo;
+    if (warp == 1 && lane == 0) w.s_hi = s_hi;
+    __syncthreads();
+    s_lo = w.s_lo;
+    s_hi = w.s_hi;
+    const bool staged = w.cached_size != 0;
+    // the anchor row walked in reverse: the live row (staged in this epoch)
+    const uint32_t ab = r.off[anc], ad = r.deg[anc];
     uint32_t par = 0;
     for (uint32_t c0 = s_lo; c0 <= s_hi; c0 += kSliceMids) {
         const uint32_t cl = min(kSliceMids, s_hi + 1 - c0);
+        uint32_t cnt = 0;
         if (threadIdx.x < cl) {
             const uint32_t slot = c0 + threadIdx.x;
             const uint32_t mid = r.nbr[pb + slot];
             const uint32_t e_pm = r.eid[pb + slot];
+            const uint32_t p0 = pre[slot];
+            const uint32_t p1 = slot + 1 < pd ? pre[slot + 1] : total;
+            const uint32_t lo = max(f0, p0), hi = min(f1, p1);
+            const uint32_t dk = p1 - p0;
+            bool ok = lo < hi && mid != anc;
+            ok = ok && prep_slot(threadIdx.x, e_pm);
+            uint32_t mask = 0, base = 0, j0 = 0;
+            if (ok) {
+                const uint32_t hm = r.hub_mask[mid];
+                if (hm && ad < dk) {  // reverse: walk anc's row, look up in mid's table
+                    mask = hm;
+                    base = r.hub_base[mid];
+                    j0 = (uint32_t)((unsigned long long)(lo - p0) * ad / dk);
+                    const uint32_t j1 = (uint32_t)((unsigned long long)(hi - p0) * ad / dk);
+                    cnt = j1 - j0;
+                } else {
+                    base = r.off[mid];
+                    j0 = lo - p0;
+                    cnt = hi - lo;
+                }
+            }
             w.mid_eid[threadIdx.x] = e_pm;
-            w.mid_base[threadIdx.x] = r.off[mid];
-            w.pre[threadIdx.x] = pre[slot];
-            w.ok[threadIdx.x] = (mid != anc && prep_slot(threadIdx.x, e_pm)) ? 1 : 0;
+            w.mid_base[threadIdx.x] = base;
+            w.mid_mask[threadIdx.x] = mask;
+            w.mid_j0[threadIdx.x] = j0;
         }
-        if (threadIdx.x == 0) w.pre[cl] = c0 + cl < pd ? pre[c0 + cl] : total;
+        uint32_t excl, tot;
+        cub::BlockScan<uint32_t, kThreads>(w.scan).ExclusiveSum(cnt, excl, tot);
+        if (threadIdx.x < cl) w.pre[threadIdx.x] = excl;
+        if (threadIdx.x == 0) {
+            w.pre[cl] = tot;
+            w.walked += tot;
+        }
         __syncthreads();
-        const uint32_t g0 = max(f0, w.pre[0]), g1 = min(f1, w.pre[cl]);
-        for (uint32_t rb = g0; rb < g1; rb += kRound) {
-            // pass 1: probe, queue hits
+        prof_mark(w, PF_SLICE);
+        for (uint32_t rb = 0; rb < tot; rb += kRound) {
+            // pass 1: walk, queue hits.  Each thread takes kPerThread
+            // consecutive positions; the steps are batched across them (all
+            // positions, then all row loads, then all lookups) so that their
+            // memory round trips overlap.
             uint32_t hk[kPerThread], hp[kPerThread], ha[kPerThread];
-            uint32_t mask = 0;
+            uint32_t hitmask = 0, act = 0, rev = 0;
+            uint32_t jp[kPerThread], yv[kPerThread], ev[kPerThread];
             const uint32_t f = rb + threadIdx.x * kPerThread;
-            if (f < g1) {
+            if (f < tot) {
                 uint32_t lo = 0, hi = cl;
                 while (hi - lo > 1) {
                     const uint32_t md = (lo + hi) >> 1;
@@ -316,26 +407,59 @@ __device__ inline void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w
 #pragma unroll
                 for (uint32_t p = 0; p < kPerThread; p++) {
                     const uint32_t ff = f + p;
-                    hk[p] = hp[p] = ha[p] = 0;
-                    if (ff < g1) {
+                    hk[p] = jp[p] = 0;
+                    if (ff < tot) {
                         while (w.pre[k + 1] <= ff) k++;
-                        if (w.ok[k]) {
-                            const uint32_t pos = w.mid_base[k] + (ff - w.pre[k]);
-                            const uint32_t y = r.nbr[pos];
-                            if (y != piv) {
-                                const uint32_t a = walk_lookup(r, w, y);
-                                if (a != kEmpty) {
-                                    hk[p] = k;
-                                    hp[p] = pos;
-                                    ha[p] = a;
-                                    mask |= 1u << p;
-                                }
-                            }
-                        }
+                        hk[p] = k;
+                        jp[p] = w.mid_j0[k] + (ff - w.pre[k]);
+                        act |= 1u << p;
+                        if (w.mid_mask[k]) rev |= 1u << p;
                     }
                 }
             }
-            const uint32_t nh = __popc(mask);
+#pragma unroll
+            for (uint32_t p = 0; p < kPerThread; p++) {
+                yv[p] = piv;
+                ev[p] = 0;
+                if (act & (1u << p)) {
+                    const uint32_t j = jp[p];
+                    if (!(rev & (1u << p))) {
+                        const uint32_t pos = w.mid_base[hk[p]] + j;
+                        yv[p] = r.nbr[pos];
+                        ev[p] = r.eid[pos];  // loaded with y: no round trip later
+                    } else if (staged) {
+                        yv[p] = w.arow[j];
+                        ev[p] = w.aslot[j];
+                    } else {
+                        yv[p] = r.nbr[ab + j];
+                        ev[p] = r.eid[ab + j];
+                    }
+                }
+            }
+#pragma unroll
+            for (uint32_t p = 0; p < kPerThread; p++) {
+                hp[p] = ha[p] = 0;
+                if (yv[p] == piv) continue;  // inactive positions carry piv
+                if (!(rev & (1u << p))) {
+                    // forward: y in mid's row, looked up in the anchor
+                    const uint32_t a = walk_lookup(r, w, yv[p]);
+                    if (a != kEmpty) {
+                        hp[p] = ev[p];
+                        ha[p] = a;
+                        hitmask |= 1u << p;
+                    }
+                } else {
+                    // reverse: y in the anchor's row, looked up in mid's hub table
+                    const uint32_t e_my = hub_lookup(r.hub_pool, w.mid_base[hk[p]], w.mid_mask[hk[p]], yv[p]);
+                    if (e_my != kEmpty) {
+                        hk[p] |= kRevHit;
+                        hp[p] = e_my;
+                        ha[p] = ev[p];
+                        hitmask |= 1u << p;
+                    }
+                }
+            }
+            const uint32_t nh = __popc(hitmask);
             uint32_t incl = nh;
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -346,7 +470,7 @@ __device__ inline void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w
             base = __shfl_sync(0xffffffffu, base, 31) + incl - nh;
 #pragma unroll
             for (uint32_t p = 0; p < kPerThread; p++) {
-                if (mask & (1u << p)) {
+                if (hitmask & (1u << p)) {
                     w.hit_k[base] = (uint16_t)hk[p];
                     w.hit_pos[base] = hp[p];
                     w.hit_a[base] = ha[p];
@@ -354,15 +478,31 @@ __device__ inline void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w
                 }
             }
             __syncthreads();
-            // pass 2: one hit per thread
+            prof_mark(w, PF_PROBE);
+            // pass 2: up to kPerThread hits per thread; hit_load issues the
+            // loads of all of them before hit_apply acts on any
             const uint32_t n = w.hit_n[par];
-            for (uint32_t i = threadIdx.x; i < n; i += kThreads) on_hit(w.hit_k[i], w.hit_pos[i], w.hit_a[i]);
+            {
+                typename OnHit::State hs[kPerThread];
+#pragma unroll
+                for (uint32_t q = 0; q < kPerThread; q++) {
+                    const uint32_t i = threadIdx.x + q * kThreads;
+                    if (i < n) on_hit.load(hs[q], w.hit_k[i], w.hit_pos[i], w.hit_a[i]);
+                }
+#pragma unroll
+                for (uint32_t q = 0; q < kPerThread; q++) {
+                    const uint32_t i = threadIdx.x + q * kThreads;
+                    if (i < n) on_hit.apply(hs[q]);
+                }
+            }
             if (threadIdx.x == 0) w.hit_n[par ^ 1] = 0;
             par ^= 1;
             __syncthreads();
+            prof_mark(w, PF_HITS);
         }
-        slice_done(cl);
+        slice_done(cl, c0 + kSliceMids > s_hi);
         __syncthreads();
+        prof_mark(w, PF_FLUSH);
     }
     if (threadIdx.x == 0) w.hit_n[0] = w.hit_n[1] = 0;
     __syncthreads();

@@ -43,6 +43,51 @@ struct HidxArgs {
     unsigned *changed;
 };
 
+// pass 1 of an edge: K = list length, cge = values >= H
+struct CountHits {
+    const unsigned long long *prev;
+    const bt::Walk &w;
+    unsigned long long H, K = 0, cge = 0;
+    struct State {
+        unsigned long long p1, p2, p3;
+    };
+    __device__ __forceinline__ void load(State &s, uint32_t kk, uint32_t e_my, uint32_t ah) const {
+        s.p1 = prev[w.mid_eid[kk & ~(uint32_t)bt::kRevHit]];
+        s.p2 = prev[e_my];
+        s.p3 = prev[bt::walk_anchor_edge(w, ah)];
+    }
+    __device__ __forceinline__ void apply(const State &s) {
+        if (s.p1 == 0 || s.p2 == 0 || s.p3 == 0) return;
+        unsigned long long v = s.p1 < s.p2 ? s.p1 : s.p2;
+        v = v < s.p3 ? v : s.p3;
+        K++;
+        if (v >= H) cge++;
+    }
+};
+
+// a refinement pass: histogram of the values in [lo, hi), count of those >= hi
+struct BinHits {
+    const unsigned long long *prev;
+    const bt::Walk &w;
+    uint32_t *hist;
+    unsigned long long lo, hi, width, above = 0;
+    struct State {
+        unsigned long long p1, p2, p3;
+    };
+    __device__ __forceinline__ void load(State &s, uint32_t kk, uint32_t e_my, uint32_t ah) const {
+        s.p1 = prev[w.mid_eid[kk & ~(uint32_t)bt::kRevHit]];
+        s.p2 = prev[e_my];
+        s.p3 = prev[bt::walk_anchor_edge(w, ah)];
+    }
+    __device__ __forceinline__ void apply(const State &s) {
+        if (s.p1 == 0 || s.p2 == 0 || s.p3 == 0) return;
+        unsigned long long v = s.p1 < s.p2 ? s.p1 : s.p2;
+        v = v < s.p3 ? v : s.p3;
+        if (v >= hi) above++;
+        else if (v >= lo) atomicAdd(&hist[(v - lo) / width], 1u);
+    }
+};
+
 struct HSmem {
     bt::Walk walk;
     uint32_t hist[kBuckets];
@@ -83,7 +128,7 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
     bt::walk_init(sm.walk);
     const unsigned long long *prev = a.prev;
     auto keep_all = [](uint32_t, uint32_t) { return true; };
-    auto no_slice = [](uint32_t) {};
+    auto no_slice = [](uint32_t, bool) {};
     bool any_change = false;
     for (;;) {
         if (threadIdx.x == 0) sm.e0 = atomicAdd(a.next_edge, (unsigned long long)kEdgeChunk);
@@ -102,19 +147,10 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
             const uint32_t piv = cv <= cu ? uv.y : uv.x, anc = cv <= cu ? uv.x : uv.y;
             const uint32_t total = a.two_hop[piv];
             // pass 1: K = list length, cge = values >= H
-            unsigned long long K = 0, cge = 0;
             bt::Walk &w = sm.walk;
-            bt::walk_range(a.rows, a.rowpre, w, piv, anc, total, 0, total, keep_all,
-                           [&](uint32_t k, uint32_t pos, uint32_t ah) {
-                               const unsigned long long p1 = prev[w.mid_eid[k]], p2 = prev[a.rows.eid[pos]],
-                                                        p3 = prev[bt::walk_anchor_edge(w, ah)];
-                               if (p1 == 0 || p2 == 0 || p3 == 0) return;
-                               unsigned long long v = p1 < p2 ? p1 : p2;
-                               v = v < p3 ? v : p3;
-                               K++;
-                               if (v >= H) cge++;
-                           },
-                           no_slice);
+            CountHits ch{prev, w, H};
+            bt::walk_range(a.rows, a.rowpre, w, piv, anc, 0, total, 0, total, keep_all, ch, no_slice);
+            unsigned long long K = ch.K, cge = ch.cge;
             block_sum2(sm, K, cge);
             unsigned long long h;
             if (cge >= H) {
@@ -132,19 +168,9 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
                     const unsigned long long width = (hi - lo + kBuckets - 1) / kBuckets;
                     for (uint32_t t = threadIdx.x; t < kBuckets; t += blockDim.x) sm.hist[t] = 0;
                     __syncthreads();
-                    unsigned long long above = 0, unused = 0;
-                    bt::walk_range(a.rows, a.rowpre, w, piv, anc, total, 0, total, keep_all,
-                                   [&](uint32_t k, uint32_t pos, uint32_t ah) {
-                                       const unsigned long long p1 = prev[w.mid_eid[k]],
-                                                                p2 = prev[a.rows.eid[pos]],
-                                                                p3 = prev[bt::walk_anchor_edge(w, ah)];
-                                       if (p1 == 0 || p2 == 0 || p3 == 0) return;
-                                       unsigned long long v = p1 < p2 ? p1 : p2;
-                                       v = v < p3 ? v : p3;
-                                       if (v >= hi) above++;
-                                       else if (v >= lo) atomicAdd(&sm.hist[(v - lo) / width], 1u);
-                                   },
-                                   no_slice);
+                    BinHits bh{prev, w, sm.hist, lo, hi, width};
+                    bt::walk_range(a.rows, a.rowpre, w, piv, anc, 0, total, 0, total, keep_all, bh, no_slice);
+                    unsigned long long above = bh.above, unused = 0;
                     block_sum2(sm, above, unused);
                     if (threadIdx.x == 0) {
                         // largest bucket b with count(values >= start_b) >= start_b

@@ -104,6 +104,7 @@ struct bt_ctx {
     double phase_ms[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
     uint64_t stats[8] = {0};
     uint64_t work[12] = {0};  // msp work counters and phase times of the last call
+    uint64_t prof[8] = {0};   // msp: SM cycles per CTA by step (task, stage, slice, probe, hits, flush, barrier, other)
     cudaEvent_t ev[8] = {};
 };
 

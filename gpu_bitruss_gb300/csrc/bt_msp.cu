@@ -14,28 +14,37 @@
 //    :110-123);
 //  * the frontier is then marked processed and the next frontier becomes the
 //    frontier of a new sub-round at the same level (:516-534);
-//  * the result is each edge's support when it was processed.
-// The order of decrements inside a sub-round does not change the result
-// (clamping makes the final value max(L, s - d)), so the GPU may apply them in
-// any order and aggregate them.
+//  * the result is each edge's support when it was processed, i.e. the level
+//    at which it joined a frontier.
+// The order of decrements inside a sub-round does not change the result, so
+// the GPU may apply them in any order and aggregate them.
 //
 // GB300 design: one cooperative persistent kernel runs the whole level /
-// sub-round loop on the device (no host round trip per sub-round; the
-// reference pays 3 syncs and ~9m bytes of copies per sub-round, :527-533).
-// Phases are separated by a grid barrier whose waits are bounded by a time
-// limit (an expired wait sets an error and the kernel returns).
-//  * Frontier discovery uses two support buckets: "near" holds the unprocessed
+// sub-round loop on the device (the reference pays 3 host syncs and ~9m bytes
+// of copies per sub-round, :527-533).
+//  * Edge state is one stamp per edge: enter[e] = the index of the sub-round
+//    whose frontier e joined (0: not yet).  In sub-round r an edge is in the
+//    frontier iff enter == r and processed iff 0 < enter < r, so "mark the
+//    frontier processed, promote the next frontier" costs nothing: the thread
+//    that pushes an edge to the next frontier stamps it r+1 and records its
+//    result (L).  A sub-round therefore needs one grid barrier.
+//  * Frontier discovery uses two support buckets: "near" holds the live
 //    edges with support < hi, "far" the rest.  A level scans only the near
 //    list; when it runs dry the far list is split again.  A decrement that
 //    crosses hi appends the edge to near.
-//  * A peeled edge is walked from the endpoint whose two-hop neighbourhood is
-//    smaller (both directions visit the same butterflies and name the four
-//    edges the same way).  Its work is split into CTA tasks over slices of the
-//    walked row; a task stages the other endpoint's row in a shared-memory
-//    hash (vertex -> edge id) and probes every neighbour list of the slice
-//    against it, with the slice's rows flattened so all threads stay busy.
+//  * Every CTA plans a small frontier itself in shared memory (orientation of
+//    each edge, tasks of equal probe counts); a large one is planned by CTA 0
+//    behind one more barrier.  Tasks are taken from a counter.
+//  * A task walks its share of the pivot's mids (bt::walk_range): anchor row
+//    in a shared hash or its hub table, each (mid, anchor) pair intersected
+//    from the shorter side, hits queued in shared memory and ruled on in a
+//    dense pass; decrements of the pivot-side and anchor-side edges are summed
+//    in shared memory and flushed once.
 //  * Processed edges are dropped from the rows (device-side compaction) with
 //    the reference's trigger (:537-549), which only changes work, not results.
+// Grid barriers are bounded by a time limit; an expired wait sets an error and
+// the kernel returns.
+#include <cstdio>
 #include <cstdlib>
 
 #include "bt_device.cuh"
@@ -44,34 +53,42 @@
 namespace {
 
 using bt::kEmpty;
-using bt::kSliceMids;
 using bt::kThreads;
-constexpr uint32_t kMinGrain = 512;         // probes per task, at least
-constexpr uint32_t kTasksPerCta = 2;        // target tasks per CTA per sub-round
-
-enum : uint8_t { ST_LIVE = 0, ST_CURR = 1, ST_DONE = 2 };
+constexpr uint32_t kMinGrain = 2048;    // plain probe positions per task, at least
+constexpr uint32_t kLocalPlan = 512;    // frontiers up to this size are planned by every CTA
 
 struct MspState {
     bt::Barrier bar;
     // control
-    unsigned long long level, hi, delta;
+    unsigned long long hi, delta;
     unsigned long long min_sup, far_min;
     long long edge_num;            // unprocessed edges
     unsigned long long live_at_compress;
     unsigned long long last_level; // last level with a non-empty frontier
-    uint32_t len[2];               // frontier lists: len[par] = current, len[par^1] = next
-    uint32_t near_len, near2_len, far_len, far2_len;
-    uint32_t task_total, task_next, done;
-    unsigned long long ph_ns[4];   // CTA 0's time in: level transitions, peel, finalize
+    uint32_t len[3];               // frontier list lengths by sub-round index mod 3
+    uint32_t task_ctr[3];          // task counters by sub-round index mod 3
+    uint32_t near_ctr[2];          // near bucket lengths (selector kept by every CTA)
+    uint32_t far_len, far2_len;
+    uint32_t task_total, done, overflow;
+    unsigned long long ph_ns[4];   // CTA 0's time in: level transitions, sub-rounds
+    unsigned long long prof[8];    // SM cycles summed over CTAs, by step (bt::PF_*)
     // statistics
     unsigned long long subrounds, compressions, tasks, levels_seen, rebuilds;
-    // work counters (algorithmic bytes): pivot slots walked, neighbour slots
-    // probed, anchor slots of the peeled edges, butterflies found, decrements
+    // work counters (algorithmic bytes): tasks, row positions walked, anchor
+    // slots of the peeled edges, butterflies found, decrements
     unsigned long long w_mids, w_probes, w_anchor, w_hits, w_decs;
 };
 
 struct Work {
     unsigned long long mids = 0, probes = 0, hits = 0, decs = 0;
+};
+
+// Optional per-sub-round trace (BT_MSP_TRACE=<path>): what bounds a sub-round.
+struct TraceRow {
+    unsigned long long t_ns;        // sub-round duration seen by CTA 0 (plan to barrier exit)
+    unsigned long long max_task_ns; // longest task
+    unsigned long long walked;      // row positions walked
+    uint32_t frontier, tasks;
 };
 
 struct MspArgs {
@@ -85,21 +102,22 @@ struct MspArgs {
     uint32_t *two_hop;              // per vertex: sum of live neighbour degrees (row probe total)
     uint32_t *rowpre;               // per slot: prefix of the row's neighbour degrees
     unsigned long long *sup;        // working supports
-    uint8_t *st;
-    uint32_t *list_a, *list_b;      // curr / next (swap by parity)
+    uint32_t *enter;                // sub-round index at which the edge joined a frontier
+    uint32_t *result;               // bitruss number per edge
+    uint32_t *list[3];              // frontier lists by sub-round index mod 3
     uint32_t *near_a, *near_b, *far_a, *far_b;
-    uint32_t *pl_piv, *pl_anc, *pl_grain, *task_start;  // plan of the frontier
+    uint32_t *pl_piv, *pl_anc, *pl_grain, *pl_total, *task_start;  // plan of a large frontier
     const uint32_t *hub_base, *hub_mask;
     const uint2 *hub_pool;
+    TraceRow *trace;                // optional, trace_cap rows
+    uint32_t trace_cap;
 };
 
 // ---------------------------------------------------------------------------
 // helpers
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ bool barrier(const MspArgs &a) {
-    return bt::grid_barrier(&a.s->bar, a.nblocks, a.wait_ns);
-}
+__device__ __forceinline__ bool is_done(uint32_t en, uint32_t r) { return en != 0 && en < r; }
 
 __device__ __forceinline__ unsigned long long warp_min(unsigned long long v) {
     for (int o = 16; o; o >>= 1) {
@@ -107,17 +125,6 @@ __device__ __forceinline__ unsigned long long warp_min(unsigned long long v) {
         v = t < v ? t : v;
     }
     return v;
-}
-
-// subtract k from sup[e]; push to the next frontier when it crosses L+1 -> L
-// and to the near bucket when it crosses hi
-__device__ __forceinline__ void dec_edge(const MspArgs &a, uint32_t *next, uint32_t *next_len,
-                                         uint32_t *near_list, unsigned long long L,
-                                         unsigned long long hi, uint32_t e, uint32_t k) {
-    unsigned long long old = atomicAdd(a.sup + e, (unsigned long long)(-(long long)k));
-    unsigned long long nw = old - k;
-    if (old > L && nw <= L) next[atomicAdd(next_len, 1u)] = e;
-    if (old >= hi && nw < hi) near_list[atomicAdd(&a.s->near_len, 1u)] = e;
 }
 
 // the peel rule for one butterfly seen from frontier edge uv; returns a 3-bit
@@ -147,22 +154,70 @@ __device__ __forceinline__ uint32_t peel_rule(uint32_t uv, uint32_t wv, uint32_t
     return d;
 }
 
+// One sub-round's view of the state.
+struct Round {
+    uint32_t r;                     // sub-round index
+    unsigned long long L, hi;       // level and near-bucket bound
+    uint32_t *next, *next_len;      // next frontier
+    uint32_t *near_list, *near_len;
+};
+
+// Subtract k from sup[e].  The decrement that takes it from above L to L or
+// below puts e in the next frontier (stamp r+1, result L): the reference's
+// clamp at L (update_edge_support, bitruss_msp.cu:110-123) then only matters
+// for the value it is processed with, which is L.  A decrement crossing hi
+// appends e to the near bucket.
+__device__ __forceinline__ void dec_edge(const MspArgs &a, const Round &rd, uint32_t e, uint32_t k) {
+    const unsigned long long old = atomicAdd(a.sup + e, (unsigned long long)(-(long long)k));
+    const unsigned long long nw = old - k;
+    if (old > rd.L && nw <= rd.L) {
+        rd.next[atomicAdd(rd.next_len, 1u)] = e;
+        a.enter[e] = rd.r + 1;
+        a.result[e] = (uint32_t)rd.L;
+    }
+    if (old >= rd.hi && nw < rd.hi) rd.near_list[atomicAdd(rd.near_len, 1u)] = e;
+}
+
 // ---------------------------------------------------------------------------
-// phases
+// shared memory
 // ---------------------------------------------------------------------------
 
 struct Smem {
     bt::Walk walk;
-    uint32_t task, idx, k;
+    // plan of a small frontier (every CTA computes it)
+    uint32_t lp_piv[kLocalPlan];
+    uint32_t lp_anc[kLocalPlan];
+    uint32_t lp_grain[kLocalPlan];
+    uint32_t lp_total[kLocalPlan];
+    uint32_t lp_start[kLocalPlan + 1];
+    uint32_t task, idx;
     uint32_t running;
     unsigned long long total;
 };
 
-// Plan the frontier (one CTA): orientation of every edge, then tasks of equal
-// probe counts.  The grain adapts to the sub-round's total work so that all
-// CTAs get tasks; an edge's grain is at least twice its anchor row (each task
-// stages that row).
-__device__ void plan_frontier(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t len) {
+__device__ __forceinline__ bool barrier(const MspArgs &a, Smem &sm) {
+    bt::prof_mark(sm.walk, bt::PF_OTHER);
+    const bool ok = bt::grid_barrier(&a.s->bar, a.nblocks, a.wait_ns);
+    bt::prof_mark(sm.walk, bt::PF_BARRIER);
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// plan: orientation of every frontier edge and tasks of equal probe counts
+// ---------------------------------------------------------------------------
+//
+// The pivot is the endpoint whose row's probe total (two_hop) is smaller.  The
+// grain is the sub-round's total over two tasks per CTA (tasks are taken
+// dynamically, so two per CTA even out their unequal real costs), at least
+// kMinGrain and, for an anchor staged in shared memory, at least twice its
+// row (each task stages that row).
+// Writes piv/anc per edge, the grain (bit 31: the pivot is the V end), the
+// pivot row's probe total and the exclusive prefix of task counts
+// (start[len] = number of tasks).  Runs on one whole CTA.
+constexpr uint32_t kPivIsV = 0x80000000u;
+__device__ void plan(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t len, uint32_t *piv_out,
+                     uint32_t *anc_out, uint32_t *grain_out, uint32_t *total_out, uint32_t *start_out,
+                     bool count_anchor) {
     if (threadIdx.x == 0) {
         sm.running = 0;
         sm.total = 0;
@@ -173,15 +228,16 @@ __device__ void plan_frontier(const MspArgs &a, Smem &sm, const uint32_t *curr, 
         const uint32_t e = curr[i];
         const uint2 uv = a.ends[e];
         const uint32_t cu = a.two_hop[uv.x], cv = a.two_hop[uv.y];
-        const uint32_t piv = cv <= cu ? uv.y : uv.x, anc = cv <= cu ? uv.x : uv.y;
-        a.pl_piv[i] = piv;
-        a.pl_anc[i] = anc;
+        piv_out[i] = cv <= cu ? uv.y : uv.x;
+        anc_out[i] = cv <= cu ? uv.x : uv.y;
+        total_out[i] = cv <= cu ? cv : cu;
+        grain_out[i] = cv <= cu ? kPivIsV : 0;
         mine += cv <= cu ? cv : cu;
     }
     for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&sm.total, mine);
     __syncthreads();
-    unsigned long long g = sm.total / ((unsigned long long)kTasksPerCta * a.nblocks);
+    unsigned long long g = sm.total / (2ull * a.nblocks);
     if (g < kMinGrain) g = kMinGrain;
     if (g > (1u << 30)) g = 1u << 30;
     unsigned long long anchor = 0;
@@ -189,125 +245,170 @@ __device__ void plan_frontier(const MspArgs &a, Smem &sm, const uint32_t *curr, 
         const uint32_t i = base + threadIdx.x;
         uint32_t nt = 0;
         if (i < len) {
-            const uint32_t piv = a.pl_piv[i], anc = a.pl_anc[i];
-            const uint32_t work = a.two_hop[piv];
+            const uint32_t anc = anc_out[i];
+            const uint32_t work = total_out[i];
             const uint32_t da = a.deg[anc];
-            unsigned long long gi = g > 2ull * da ? g : 2ull * da;
-            if (gi > (1u << 30)) gi = 1u << 30;
+            // a task stages a short anchor row in shared memory: make it worth it
+            unsigned long long gi = (da <= bt::kHashMaxDeg && 2ull * da > g) ? 2ull * da : g;
+            if (gi > (1u << 30)) gi = 1u << 30;  // leaves bit 31 for kPivIsV
             nt = (uint32_t)((work + gi - 1) / gi);
-            a.pl_grain[i] = (uint32_t)gi;
+            grain_out[i] |= (uint32_t)gi;
             anchor += da;
         }
         uint32_t excl, tot;
         cub::BlockScan<uint32_t, kThreads>(sm.walk.scan).ExclusiveSum(nt, excl, tot);
-        if (i < len) a.task_start[i] = sm.running + excl;
+        if (i < len) start_out[i] = sm.running + excl;
         __syncthreads();
         if (threadIdx.x == 0) sm.running += tot;
         __syncthreads();
     }
-    for (int o = 16; o; o >>= 1) anchor += __shfl_xor_sync(0xffffffffu, anchor, o);
-    if ((threadIdx.x & 31) == 0 && anchor) atomicAdd(&a.s->w_anchor, anchor);
-    if (threadIdx.x == 0) {
-        a.task_start[len] = sm.running;
-        a.s->task_total = sm.running;
-        a.s->task_next = 0;
+    if (threadIdx.x == 0) start_out[len] = sm.running;
+    if (count_anchor) {
+        for (int o = 16; o; o >>= 1) anchor += __shfl_xor_sync(0xffffffffu, anchor, o);
+        if ((threadIdx.x & 31) == 0 && anchor) atomicAdd(&a.s->w_anchor, anchor);
     }
+    __syncthreads();
 }
 
-// Peel all tasks of the current sub-round.
+// ---------------------------------------------------------------------------
+// peel: all tasks of one sub-round
+// ---------------------------------------------------------------------------
+
+// The rule applied to the butterflies of one frontier edge uv (see
+// bt::walk_range for the two-step interface).
+struct MspHit {
+    const MspArgs &a;
+    bt::Walk &w;
+    const Round &rd;
+    uint32_t uv, exact;
+    bool piv_is_v;
+    unsigned long long decs = 0;
+    struct State {
+        uint32_t kslot, e_my, e_ay, ah, en_my, en_ay;
+    };
+    __device__ __forceinline__ void load(State &s, uint32_t kk, uint32_t e_my, uint32_t ah) const {
+        s.kslot = kk & ~(uint32_t)bt::kRevHit;
+        s.e_my = e_my;
+        s.ah = ah;
+        s.e_ay = bt::walk_anchor_edge(w, ah);
+        s.en_my = a.enter[e_my];
+        s.en_ay = a.enter[s.e_ay];
+    }
+    __device__ __forceinline__ void apply(const State &s) {
+        const uint32_t r = rd.r;
+        if (is_done(s.en_ay, r) || is_done(s.en_my, r)) return;
+        const uint32_t e_pm = w.mid_eid[s.kslot];
+        const bool c_pm = w.pm_curr[s.kslot], c_my = s.en_my == r, c_ay = s.en_ay == r;
+        // name the edges as the reference does: w on u's side, x on v's
+        uint32_t wv, ux;
+        bool cwv, cux;
+        if (piv_is_v) { wv = e_pm; ux = s.e_ay; cwv = c_pm; cux = c_ay; }
+        else { wv = s.e_ay; ux = e_pm; cwv = c_ay; cux = c_pm; }
+        const uint32_t d = peel_rule(uv, wv, s.e_my, ux, cwv, c_my, cux, exact);
+        if (!d) return;
+        const bool d_wv = d & 1, d_wx = d & 2, d_ux = d & 4;
+        const bool dec_pm = piv_is_v ? d_wv : d_ux;
+        const bool dec_ay = piv_is_v ? d_ux : d_wv;
+        decs += (uint32_t)dec_pm + (uint32_t)d_wx + (uint32_t)dec_ay;
+        if (dec_pm) atomicAdd(&w.slot_dec[s.kslot], 1u);
+        if (d_wx) dec_edge(a, rd, s.e_my, 1);
+        if (dec_ay) {
+            if (w.cached_size) atomicAdd(&w.hdec[s.ah], 1u);
+            else dec_edge(a, rd, s.e_ay, 1);
+        }
+    }
+};
+
 __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t curr_len,
-                           uint32_t *next, uint32_t *next_len, uint32_t *near_list,
-                           unsigned long long L, unsigned long long hi, Work &wk) {
+                           const uint32_t *pl_piv, const uint32_t *pl_anc, const uint32_t *pl_grain,
+                           const uint32_t *pl_total, const uint32_t *start, uint32_t ntasks, uint32_t *ctr,
+                           const Round &rd, uint32_t epoch, Work &wk) {
     const bt::Rows rows{a.off, a.deg, a.nbr, a.eid, a.hub_base, a.hub_mask, a.hub_pool};
-    const uint8_t *st = a.st;
-    const uint32_t ntasks = a.s->task_total;
-    for (uint32_t t = blockIdx.x; t < ntasks; t += gridDim.x) {
-        // frontier edge of task t: last i with task_start[i] <= t
+    const uint32_t *enter = a.enter;
+    const uint32_t r = rd.r;
+    const uint32_t lane = threadIdx.x & 31;
+    bt::Walk &w = sm.walk;
+    bool first = true;
+    for (;;) {
         if (threadIdx.x < 32) {
-            const uint32_t i = bt::warp_find_slot(a.task_start, curr_len, t);
-            if (threadIdx.x == 0) {
+            // the first task of every CTA is its block index; the rest come
+            // from the counter, which starts at the number of CTAs
+            uint32_t t = blockIdx.x;
+            if (!first && lane == 0) t = gridDim.x + atomicAdd(ctr, 1u);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            uint32_t i = 0;
+            if (t < ntasks) i = bt::warp_find_slot(start, curr_len, t);  // last i: start[i] <= t
+            if (lane == 0) {
+                sm.task = t;
                 sm.idx = i;
-                sm.k = t - a.task_start[i];
             }
         }
         __syncthreads();
-        const uint32_t i = sm.idx, k = sm.k;
+        first = false;
+        const uint32_t t = sm.task;
+        if (t >= ntasks) break;
+        const unsigned long long task_t0 = (a.trace && threadIdx.x == 0) ? bt::global_ns() : 0;
+        const unsigned long long walked0 = w.walked;
+        const uint32_t i = sm.idx, k = t - start[i];
         const uint32_t uv = curr[i];
-        const uint32_t piv = a.pl_piv[i], anc = a.pl_anc[i], gi = a.pl_grain[i];
-        const bool piv_is_v = (piv == a.ends[uv].y);
-        const uint32_t total = a.two_hop[piv];
+        const uint32_t piv = pl_piv[i], anc = pl_anc[i], gword = pl_grain[i];
+        const uint32_t gi = gword & ~kPivIsV, total = pl_total[i];
+        const bool piv_is_v = (gword & kPivIsV) != 0;
         const uint32_t f0 = k * gi;
         const uint32_t f1 = total - f0 < gi ? total : f0 + gi;
         const uint32_t exact = a.exact;
         if (threadIdx.x == 0) wk.mids++;
-        bt::Walk &w = sm.walk;
+        bt::prof_mark(w, bt::PF_TASK);
+        MspHit hit{a, w, rd, uv, exact, piv_is_v};
         bt::walk_range(
-            rows, a.rowpre, w, piv, anc, total, f0, f1,
-            [&](uint32_t k, uint32_t e_pm) {
-                const uint8_t sp = st[e_pm];
-                w.pm_curr[k] = sp == ST_CURR;
-                return sp != ST_DONE;
+            rows, a.rowpre, w, piv, anc, epoch, total, f0, f1,
+            [&](uint32_t kk, uint32_t e_pm) {
+                const uint32_t en = enter[e_pm];
+                w.pm_curr[kk] = en == r;
+                return !is_done(en, r);
             },
-            [&](uint32_t k, uint32_t pos, uint32_t ah) {
-                const uint32_t e_pm = w.mid_eid[k];
-                const uint32_t e_ay = bt::walk_anchor_edge(w, ah);
-                const uint32_t e_my = a.eid[pos];
-                const uint8_t s_ay = st[e_ay], s_my = st[e_my];
-                wk.hits++;
-                if (s_ay == ST_DONE || s_my == ST_DONE) return;
-                const bool c_pm = w.pm_curr[k], c_my = s_my == ST_CURR, c_ay = s_ay == ST_CURR;
-                // name the edges as the reference does: w on u's side, x on v's
-                uint32_t wv, ux;
-                bool cwv, cux;
-                if (piv_is_v) { wv = e_pm; ux = e_ay; cwv = c_pm; cux = c_ay; }
-                else { wv = e_ay; ux = e_pm; cwv = c_ay; cux = c_pm; }
-                const uint32_t d = peel_rule(uv, wv, e_my, ux, cwv, c_my, cux, exact);
-                if (!d) return;
-                const bool d_wv = d & 1, d_wx = d & 2, d_ux = d & 4;
-                const bool dec_pm = piv_is_v ? d_wv : d_ux;
-                const bool dec_ay = piv_is_v ? d_ux : d_wv;
-                wk.decs += (uint32_t)dec_pm + (uint32_t)d_wx + (uint32_t)dec_ay;
-                if (dec_pm) atomicAdd(&w.slot_dec[k], 1u);
-                if (d_wx) dec_edge(a, next, next_len, near_list, L, hi, e_my, 1);
-                if (dec_ay) {
-                    if (w.cached_size) atomicAdd(&w.hdec[ah], 1u);
-                    else dec_edge(a, next, next_len, near_list, L, hi, e_ay, 1);
-                }
-            },
-            [&](uint32_t cl) {
+            hit,
+            [&](uint32_t cl, bool last) {
+                // flush the pivot-side decrements of the slice and, after the
+                // last slice, the anchor-side decrements of the task
                 __syncthreads();
                 if (threadIdx.x < cl) {
                     const uint32_t c = w.slot_dec[threadIdx.x];
                     if (c) {
                         w.slot_dec[threadIdx.x] = 0;
-                        dec_edge(a, next, next_len, near_list, L, hi, w.mid_eid[threadIdx.x], c);
+                        dec_edge(a, rd, w.mid_eid[threadIdx.x], c);
+                    }
+                }
+                if (last && w.cached_size) {
+                    for (uint32_t h = threadIdx.x; h < w.cached_size; h += kThreads) {
+                        const uint32_t c = w.hdec[h];
+                        if (c) {
+                            w.hdec[h] = 0;
+                            dec_edge(a, rd, w.hval[h], c);
+                        }
                     }
                 }
             });
-        // flush the anchor-side decrements of this task
-        if (w.cached_size) {
-            for (uint32_t h = threadIdx.x; h < w.cached_size; h += kThreads) {
-                const uint32_t c = w.hdec[h];
-                if (c) {
-                    w.hdec[h] = 0;
-                    dec_edge(a, next, next_len, near_list, L, hi, w.hval[h], c);
-                }
-            }
+        wk.decs += hit.decs;
+        bt::prof_mark(w, bt::PF_FLUSH);
+        if (a.trace && threadIdx.x == 0 && r < a.trace_cap) {
+            atomicMax(&a.trace[r].max_task_ns, bt::global_ns() - task_t0);
+            atomicAdd(&a.trace[r].walked, w.walked - walked0);
         }
-        if (threadIdx.x == 0) wk.probes += f1 - f0;
-        __syncthreads();
     }
-    __syncthreads();
 }
 
+// ---------------------------------------------------------------------------
+// level transition helpers
+// ---------------------------------------------------------------------------
+
 // Minimum support over the live entries of `list` (grid-wide atomicMin).
-__device__ void list_min(const MspArgs &a, Smem &sm, const uint32_t *list, uint32_t len,
-                         unsigned long long *out) {
+__device__ void list_min(const MspArgs &a, const uint32_t *list, uint32_t len, unsigned long long *out) {
     unsigned long long v = ~0ull;
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gsz = gridDim.x * blockDim.x;
     for (uint32_t i = gtid; i < len; i += gsz) {
         const uint32_t e = list[i];
-        if (a.st[e] != ST_DONE) {
+        if (a.enter[e] == 0) {
             const unsigned long long s = a.sup[e];
             v = s < v ? s : v;
         }
@@ -316,8 +417,9 @@ __device__ void list_min(const MspArgs &a, Smem &sm, const uint32_t *list, uint3
     if ((threadIdx.x & 31) == 0 && v != ~0ull) atomicMin(out, v);
 }
 
-// Drop processed edges from every row; one warp per vertex, in place.
-__device__ void compress_rows(const MspArgs &a) {
+// Drop processed edges (enter in (0, r)) from every row; one warp per vertex,
+// in place.
+__device__ void compress_rows(const MspArgs &a, uint32_t r) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -331,7 +433,7 @@ __device__ void compress_rows(const MspArgs &a) {
             if (j < d) {
                 y = a.nbr[b + j];
                 e = a.eid[b + j];
-                keep = a.st[e] != ST_DONE;
+                keep = !is_done(a.enter[e], r);
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, keep);
             __syncwarp();
@@ -356,18 +458,17 @@ __device__ void compute_two_hop(const MspArgs &a) {
 // the persistent kernel
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kThreads, 2) k_msp(MspArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
     MspState *s = a.s;
     bt::walk_init(sm.walk);
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gsz = gridDim.x * blockDim.x;
     constexpr uint32_t kNearTarget = 1u << 16;
-    uint32_t *lists[2] = {a.list_a, a.list_b};
     Work wk;
-    uint32_t par = 0;  // lists[par] is the frontier, lists[par ^ 1] the next frontier
-    if (gtid == 0) s->min_sup = ~0ull;
-    if (!barrier(a)) return;
+    uint32_t r = 2;            // sub-round index (1 marks the zero-support edges)
+    uint32_t epoch = 0;        // row compactions so far (same in every CTA)
+    unsigned long long L = 0;  // current level (same in every CTA)
     unsigned long long t_mark = gtid == 0 ? bt::global_ns() : 0;
     auto lap = [&](int k) {
         if (gtid == 0) {
@@ -376,117 +477,148 @@ __global__ void __launch_bounds__(kThreads, 2) k_msp(MspArgs a) {
             t_mark = t;
         }
     };
+    if (!barrier(a, sm)) return;
 
+    uint32_t nsel = 0;         // near bucket: list near_a, length near_ctr[nsel]
     for (;;) {
         // ------------------------------------------------ level transition
-        if (s->len[par] == 0) {
-            // T1: min over the near bucket (min_sup was reset before the barrier)
-            list_min(a, sm, a.near_a, s->near_len, &s->min_sup);
-            if (!barrier(a)) return;
+        if (s->len[r % 3] == 0) {
+            // T1: min over the near bucket (min_sup was reset in the last sub-round)
+            list_min(a, a.near_a, s->near_ctr[nsel], &s->min_sup);
+            if (!barrier(a, sm)) return;
             if (s->min_sup == ~0ull) {
                 // T2: near is dry -> split the far bucket
-                list_min(a, sm, a.far_a, s->far_len, &s->far_min);
-                if (!barrier(a)) return;
+                list_min(a, a.far_a, s->far_len, &s->far_min);
+                if (!barrier(a, sm)) return;
                 const unsigned long long lo = s->far_min;
                 if (lo == ~0ull) break;  // nothing left
                 const unsigned long long hi = lo + s->delta;
                 for (uint32_t i = gtid; i < s->far_len; i += gsz) {
                     const uint32_t e = a.far_a[i];
-                    if (a.st[e] == ST_DONE) continue;
-                    if (a.sup[e] < hi) a.near_b[atomicAdd(&s->near2_len, 1u)] = e;
+                    if (a.enter[e] != 0) continue;
+                    if (a.sup[e] < hi) a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
                     else a.far_b[atomicAdd(&s->far2_len, 1u)] = e;
                 }
-                if (!barrier(a)) return;
+                if (!barrier(a, sm)) return;
                 {   // every CTA swaps its copies of the bucket pointers
                     uint32_t *t = a.near_a; a.near_a = a.near_b; a.near_b = t;
                     t = a.far_a; a.far_a = a.far_b; a.far_b = t;
                 }
+                nsel ^= 1;
                 if (gtid == 0) {
-                    s->near_len = s->near2_len;
+                    s->near_ctr[nsel ^ 1] = 0;
                     s->far_len = s->far2_len;
-                    s->near2_len = 0;
                     s->far2_len = 0;
                     s->hi = hi;
                     s->min_sup = lo;
                     s->far_min = ~0ull;
                     s->rebuilds++;
-                    if (s->near_len > 4 * kNearTarget && s->delta > 1) s->delta >>= 1;
-                    else if (s->near_len < kNearTarget / 4) s->delta <<= 1;
+                    if (s->near_ctr[nsel] > 4 * kNearTarget && s->delta > 1) s->delta >>= 1;
+                    else if (s->near_ctr[nsel] < kNearTarget / 4) s->delta <<= 1;
                 }
-                if (!barrier(a)) return;
+                if (!barrier(a, sm)) return;
             }
-            // T3: frontier = near edges with support == L; compact near
-            const unsigned long long L = s->min_sup;
-            const uint32_t near_len = s->near_len;
+            // T3: frontier of sub-round r = near edges with support == L; the
+            // rest of the live near edges are compacted into the other list
+            L = s->min_sup;
+            const uint32_t near_len = s->near_ctr[nsel];
+            uint32_t *front = a.list[r % 3];
             for (uint32_t i = gtid; i < near_len; i += gsz) {
                 const uint32_t e = a.near_a[i];
-                if (a.st[e] == ST_DONE) continue;
+                if (a.enter[e] != 0) continue;
                 if (a.sup[e] == L) {
-                    a.st[e] = ST_CURR;
-                    lists[par][atomicAdd(&s->len[par], 1u)] = e;
+                    a.enter[e] = r;
+                    a.result[e] = (uint32_t)L;
+                    front[atomicAdd(&s->len[r % 3], 1u)] = e;
                 } else {
-                    a.near_b[atomicAdd(&s->near2_len, 1u)] = e;
+                    a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
                 }
             }
             // T4: compression (reference trigger, bitruss_msp.cu:537)
             const bool squeeze = (double)s->edge_num <= 0.5 * (double)s->live_at_compress &&
                                  (double)s->live_at_compress >= 0.1 * (double)a.m;
-            if (!barrier(a)) return;
+            if (!barrier(a, sm)) return;
             {
                 uint32_t *t = a.near_a; a.near_a = a.near_b; a.near_b = t;
             }
-            if (squeeze) {
-                compress_rows(a);
-                if (!barrier(a)) return;
-                compute_two_hop(a);
-                if (!barrier(a)) return;
-            }
-            // T5: plan the frontier; publish the level
-            if (blockIdx.x == 0) plan_frontier(a, sm, lists[par], s->len[par]);
+            nsel ^= 1;
             if (gtid == 0) {
-                s->near_len = s->near2_len;
-                s->near2_len = 0;
-                s->level = L;
                 s->last_level = L;
                 s->levels_seen++;
+                if (L > 0xffffffffull) s->overflow = 1;
                 if (squeeze) {
                     s->live_at_compress = (unsigned long long)s->edge_num;
                     s->compressions++;
                 }
             }
-            if (!barrier(a)) return;
+            if (squeeze) {
+                compress_rows(a, r);
+                if (!barrier(a, sm)) return;
+                compute_two_hop(a);
+                epoch++;
+                if (!barrier(a, sm)) return;
+            }
             lap(0);
         }
-        // ------------------------------------------------ sub-round
-        const unsigned long long L = s->level, hi = s->hi;
-        const uint32_t curr_len = s->len[par];
-        uint32_t *curr = lists[par], *next = lists[par ^ 1];
-        peel_tasks(a, sm, curr, curr_len, next, &s->len[par ^ 1], a.near_a, L, hi, wk);
-        if (!barrier(a)) return;
-        lap(1);
-        // finalize: frontier -> processed, next -> frontier (clamped at L)
-        const uint32_t next_len = s->len[par ^ 1];
-        for (uint32_t i = gtid; i < curr_len; i += gsz) a.st[curr[i]] = ST_DONE;
-        for (uint32_t i = gtid; i < next_len; i += gsz) {
-            const uint32_t e = next[i];
-            a.st[e] = ST_CURR;
-            a.sup[e] = L;
+        // ------------------------------------------------ sub-round r
+        const unsigned long long sr_t0 = (a.trace && gtid == 0) ? bt::global_ns() : 0;
+        const uint32_t curr_len = s->len[r % 3];
+        const uint32_t *curr = a.list[r % 3];
+        Round rd;
+        rd.r = r;
+        rd.L = L;
+        rd.hi = s->hi;
+        rd.next = a.list[(r + 1) % 3];
+        rd.next_len = &s->len[(r + 1) % 3];
+        rd.near_list = a.near_a;
+        rd.near_len = &s->near_ctr[nsel];
+        uint32_t ntasks;
+        if (curr_len <= kLocalPlan) {
+            plan(a, sm, curr, curr_len, sm.lp_piv, sm.lp_anc, sm.lp_grain, sm.lp_total, sm.lp_start,
+                 blockIdx.x == 0);
+            ntasks = sm.lp_start[curr_len];
+            if (gtid == 0) s->tasks += ntasks;
+        } else {
+            if (blockIdx.x == 0) {
+                plan(a, sm, curr, curr_len, a.pl_piv, a.pl_anc, a.pl_grain, a.pl_total, a.task_start, true);
+                if (threadIdx.x == 0) {
+                    s->task_total = a.task_start[curr_len];
+                    s->tasks += s->task_total;
+                }
+            }
+            if (!barrier(a, sm)) return;
+            ntasks = s->task_total;
         }
         if (gtid == 0) {
-            s->tasks += s->task_total;
+            // slots used two sub-rounds from now; every CTA is past their last use
+            s->len[(r + 2) % 3] = 0;
+            s->task_ctr[(r + 2) % 3] = 0;
+            s->near_ctr[nsel ^ 1] = 0;  // the compaction target of the next transition
+            s->min_sup = ~0ull;
             s->edge_num -= curr_len;
             s->subrounds++;
-            s->len[par] = 0;      // every CTA holds curr_len in a register
-            if (next_len == 0) s->min_sup = ~0ull;
         }
-        __syncthreads();
-        if (blockIdx.x == 0 && next_len) plan_frontier(a, sm, next, next_len);
-        par ^= 1;
-        if (!barrier(a)) return;
-        lap(2);
+        if (curr_len <= kLocalPlan)
+            peel_tasks(a, sm, curr, curr_len, sm.lp_piv, sm.lp_anc, sm.lp_grain, sm.lp_total, sm.lp_start,
+                       ntasks, &s->task_ctr[r % 3], rd, epoch, wk);
+        else
+            peel_tasks(a, sm, curr, curr_len, a.pl_piv, a.pl_anc, a.pl_grain, a.pl_total, a.task_start,
+                       ntasks, &s->task_ctr[r % 3], rd, epoch, wk);
+        if (!barrier(a, sm)) return;
+        if (a.trace && gtid == 0 && r < a.trace_cap) {
+            a.trace[r].t_ns = bt::global_ns() - sr_t0;
+            a.trace[r].frontier = curr_len;
+            a.trace[r].tasks = ntasks;
+        }
+        lap(1);
+        r++;
     }
     if (gtid == 0) s->done = 1;
-    // flush the work counters (one atomic per warp)
+    // flush the counters
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 8; q++) atomicAdd(&s->prof[q], sm.walk.prof[q]);
+        wk.probes += sm.walk.walked;
+    }
     for (int o = 16; o; o >>= 1) {
         wk.mids += __shfl_xor_sync(0xffffffffu, wk.mids, o);
         wk.probes += __shfl_xor_sync(0xffffffffu, wk.probes, o);
@@ -506,15 +638,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_msp(MspArgs a) {
 // ---------------------------------------------------------------------------
 
 __global__ void k_msp_init(uint64_t m, const unsigned long long *sup_in, unsigned long long *sup,
-                           uint8_t *st, uint32_t *far_list, MspState *s) {
+                           uint32_t *enter, uint32_t *result, uint32_t *far_list, MspState *s) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
          e += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long v = sup_in[e];
         sup[e] = v;
+        result[e] = 0;
         if (v == 0) {
-            st[e] = ST_DONE;  // count_es_zero, bitruss_msp.cu:38-50
+            enter[e] = 1;  // processed first (count_es_zero, bitruss_msp.cu:38-50)
         } else {
-            st[e] = ST_LIVE;
+            enter[e] = 0;
             far_list[atomicAdd(&s->far_len, 1u)] = (uint32_t)e;
         }
     }
@@ -522,18 +655,11 @@ __global__ void k_msp_init(uint64_t m, const unsigned long long *sup_in, unsigne
 
 __global__ void k_two_hop(MspArgs a) { compute_two_hop(a); }
 
-__global__ void k_msp_result(uint64_t m, const unsigned long long *sup, uint32_t *out, MspState *s) {
-    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
-         e += (uint64_t)gridDim.x * blockDim.x) {
-        const unsigned long long v = sup[e];
-        if (v > 0xffffffffull) atomicCAS(&s->bar.error, 0u, (unsigned)bt::ERR_OVERFLOW);
-        out[e] = (uint32_t)v;
-    }
-}
-
 }  // namespace
 
 static unsigned long long wait_limit_ns() {
+    const char *us = getenv("BT_WAIT_LIMIT_US");
+    if (us && strtoull(us, nullptr, 10) > 0) return strtoull(us, nullptr, 10) * 1000ull;
     const char *v = getenv("BT_WAIT_LIMIT_MS");
     unsigned long long ms = v ? strtoull(v, nullptr, 10) : 120000ull;
     if (ms == 0) ms = 120000ull;
@@ -549,8 +675,6 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     cudaEvent_t e0 = ctx->ev[2], e1 = ctx->ev[3];
     cudaEventRecord(e0, st);
 
-    // working buffers
-    struct Buf { void *p = nullptr; };
     std::vector<void *> owned;
     auto alloc = [&](void **p, uint64_t bytes) -> bt_status {
         bt_status r = ctx_alloc(ctx, p, bytes);
@@ -576,9 +700,10 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     A(a.eid, 8 * mm);
     A(a.two_hop, 4 * nn);
     A(a.sup, 8 * mm);
-    A(a.st, mm);
-    A(a.list_a, 4 * mm);
-    A(a.list_b, 4 * mm);
+    A(a.enter, 4 * mm);
+    A(a.list[0], 4 * mm);
+    A(a.list[1], 4 * mm);
+    A(a.list[2], 4 * mm);
     A(a.near_a, 4 * mm);
     A(a.near_b, 4 * mm);
     A(a.far_a, 4 * mm);
@@ -586,15 +711,21 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     A(a.pl_piv, 4 * mm);
     A(a.pl_anc, 4 * mm);
     A(a.pl_grain, 4 * mm);
+    A(a.pl_total, 4 * mm);
     A(a.rowpre, 8 * mm);
     A(a.task_start, 4 * (mm + 1));
+    const char *trace_path = getenv("BT_MSP_TRACE");
+    if (trace_path && *trace_path) {
+        a.trace_cap = 4u << 20;
+        A(a.trace, sizeof(TraceRow) * a.trace_cap);
+    }
 #undef A
+    a.result = ctx->result;
 #define C(x)                                                                  \
     do {                                                                      \
         cudaError_t _e = (x);                                                 \
         if (_e != cudaSuccess) { release(); return bt_cuda_fail(_e, #x, __FILE__, __LINE__); } \
     } while (0)
-    C(cudaMemsetAsync(s, 0, sizeof(MspState), st));
     {
         MspState init{};
         init.delta = 1;
@@ -603,8 +734,9 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
         init.far_min = ~0ull;
         init.live_at_compress = m;
         C(cudaMemcpyAsync(s, &init, sizeof(MspState), cudaMemcpyHostToDevice, st));
-        C(cudaStreamSynchronize(st));
+        C(cudaStreamSynchronize(st));  // `init` lives on the host stack
     }
+    if (a.trace) C(cudaMemsetAsync(a.trace, 0, sizeof(TraceRow) * a.trace_cap, st));
     C(cudaMemcpyAsync(a.deg, g.deg0, 4 * n, cudaMemcpyDeviceToDevice, st));
     C(cudaMemcpyAsync(a.nbr, g.nbr0, 8 * m, cudaMemcpyDeviceToDevice, st));
     C(cudaMemcpyAsync(a.eid, g.eid0, 8 * m, cudaMemcpyDeviceToDevice, st));
@@ -621,7 +753,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (m) {
         k_msp_init<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
-            m, (const unsigned long long *)ctx->sup, a.sup, a.st, a.far_a, s);
+            m, (const unsigned long long *)ctx->sup, a.sup, a.enter, a.result, a.far_a, s);
         C(cudaGetLastError());
     }
     // edge_num = live edges
@@ -649,14 +781,21 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
         C(cudaLaunchCooperativeKernel((void *)k_msp, dim3(a.nblocks), dim3(kThreads), params, smem, st));
         C(cudaGetLastError());
         cudaEventRecord(ctx->ev[5], st);
-        k_msp_result<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
-            m, a.sup, ctx->result, s);
-        C(cudaGetLastError());
     }
     cudaEventRecord(e1, st);
     MspState h{};
     C(cudaMemcpyAsync(&h, s, sizeof(MspState), cudaMemcpyDeviceToHost, st));
     C(cudaStreamSynchronize(st));
+    if (a.trace) {
+        // rows 2 .. subrounds+1 are sub-rounds; written as raw TraceRow records
+        const uint64_t rows = std::min<uint64_t>(h.subrounds + 2, a.trace_cap);
+        std::vector<TraceRow> tr(rows);
+        C(cudaMemcpy(tr.data(), a.trace, sizeof(TraceRow) * rows, cudaMemcpyDeviceToHost));
+        if (FILE *f = fopen(trace_path, "wb")) {
+            fwrite(tr.data(), sizeof(TraceRow), rows, f);
+            fclose(f);
+        }
+    }
 #undef C
     float ms = -1;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -667,8 +806,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     release();
     if (h.bar.error == bt::ERR_TIMEOUT)
         return bt_fail(BT_ERR_TIMEOUT, "msp: a grid barrier wait exceeded its time limit");
-    if (h.bar.error == bt::ERR_OVERFLOW)
-        return bt_fail(BT_ERR_OVERFLOW, "msp: a bitruss number exceeds uint32");
+    if (h.overflow) return bt_fail(BT_ERR_OVERFLOW, "msp: a bitruss number exceeds uint32");
     if (m && !h.done) return bt_fail(BT_ERR_CUDA, "msp kernel ended without finishing");
     ctx->stats[0] = h.last_level;
     ctx->stats[1] = h.subrounds;
@@ -684,7 +822,8 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     ctx->work[5] = m;
     ctx->work[6] = h.ph_ns[0];
     ctx->work[7] = h.ph_ns[1];
-    ctx->work[8] = h.ph_ns[2];
+    ctx->work[8] = 0;
+    for (int q = 0; q < 8; q++) ctx->prof[q] = h.prof[q] / (a.nblocks ? a.nblocks : 1);
     ctx->last_result = 2;
     if (levels) *levels = (uint32_t)h.last_level;
     return BT_OK;

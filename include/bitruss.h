@@ -144,7 +144,9 @@ double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
  * [6] bucket splits; msp work: [8] peel tasks run, [9] neighbour slots
  * probed, [10] anchor slots, [11] butterflies found, [12] decrements, [13] m;
  * [14..16] nanoseconds the peeling kernel spent in level transitions, peel
- * phases and finalize phases. */
+ * phases and finalize phases; [20..27] SM cycles per CTA of the peeling
+ * kernel by step: task lookup, anchor staging, slice load, probe pass, hit
+ * pass, flushes, grid-barrier waits, other work. */
 bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n);
 
 /* ---- allocation-free variant ------------------------------------------ */
