@@ -16,7 +16,6 @@ constexpr uint32_t kHubMinDeg = 256;        // rows longer than this get a globa
 constexpr uint32_t kSliceMids = kThreads;   // mids per slice (one block scan)
 constexpr uint32_t kPerThread = 4;          // consecutive probes per thread per round
 constexpr uint32_t kRound = kThreads * kPerThread;
-constexpr uint32_t kHitCap = kRound;        // a round finds at most kRound butterflies
 constexpr uint32_t kEmpty = 0xffffffffu;
 
 // ---------------------------------------------------------------------------
@@ -115,11 +114,6 @@ struct Walk {
     uint32_t pre[kSliceMids + 1];    // prefix of the positions walked per slot
     uint32_t slot_dec[kSliceMids];
     uint8_t pm_curr[kSliceMids];
-    // butterflies found in the current round
-    uint16_t hit_k[kHitCap];         // slot, | kRevHit when found walking anc's row
-    uint32_t hit_pos[kHitCap];       // edge id (mid, y)
-    uint32_t hit_a[kHitCap];
-    uint32_t hit_n[2];
     uint32_t cached_anc, cached_size;  // staged anchor; size 0: use its hub table
     uint32_t cached_deg;               // length of arow
     uint32_t cached_epoch;             // row-compaction epoch the anchor was staged in
@@ -160,7 +154,6 @@ __device__ inline void walk_init(Walk &w) {
         w.cached_anc = kEmpty;
         w.cached_size = 0;
         w.cached_epoch = 0;
-        w.hit_n[0] = w.hit_n[1] = 0;
         for (int k = 0; k < 8; k++) w.prof[k] = 0;
         w.walked = 0;
         w.prof_t = clock64();
@@ -312,12 +305,12 @@ __device__ inline uint32_t warp_find_slot(const uint32_t *pre, uint32_t d, uint3
 //
 // Slices of at most kSliceMids pivot slots are loaded into shared memory;
 // prep_slot(k, e_pm) runs once per slot and says whether to walk its mid
-// (the walk itself skips mid == anc).  Each round walks kRound positions
-// (kPerThread consecutive ones per thread) and queues the hits -- y != piv
-// adjacent to both mid and anc -- in shared memory; a second pass hands every
-// hit to on_hit with all threads busy, in two steps so that the memory
-// traffic of several hits overlaps: on_hit.load(state, k, e_my, a) (loads
-// only) for up to kPerThread hits, then on_hit.apply(state) for each.  k =
+// (the walk itself skips mid == anc).  Each warp then walks stretches of
+// 32 * kPerThread positions (kPerThread consecutive ones per lane) on its own
+// and hands every hit -- y != piv adjacent to both mid and anc -- to on_hit
+// right away, in two steps so that the memory traffic of a lane's hits
+// overlaps: on_hit.load(state, k, e_my, a) (loads only) for all of them, then
+// on_hit.apply(state) for each.  k =
 // slice slot of mid (| kRevHit for a reverse hit), e_my = the edge id
 // (mid, y), a = the anchor's answer for y (walk_lookup's convention: a hash
 // slot when anc is staged, else the edge id).  slice_done(cl, last) runs
@@ -387,15 +380,14 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
         }
         __syncthreads();
         prof_mark(w, PF_SLICE);
-        for (uint32_t rb = 0; rb < tot; rb += kRound) {
-            // pass 1: walk, queue hits.  Each thread takes kPerThread
-            // consecutive positions; the steps are batched across them (all
-            // positions, then all row loads, then all lookups) so that their
-            // memory round trips overlap.
+        // Warps walk independent stretches of 32 * kPerThread positions
+        // (kPerThread consecutive ones per lane) and act on their own hits
+        // at once: no block-wide synchronisation until the slice is done.
+        for (uint32_t wb = warp * (32 * kPerThread); wb < tot; wb += kRound) {
             uint32_t hk[kPerThread], hp[kPerThread], ha[kPerThread];
             uint32_t hitmask = 0, act = 0, rev = 0;
             uint32_t jp[kPerThread], yv[kPerThread], ev[kPerThread];
-            const uint32_t f = rb + threadIdx.x * kPerThread;
+            const uint32_t f = wb + lane * kPerThread;
             if (f < tot) {
                 uint32_t lo = 0, hi = cl;
                 while (hi - lo > 1) {
@@ -459,53 +451,21 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
                     }
                 }
             }
-            const uint32_t nh = __popc(hitmask);
-            uint32_t incl = nh;
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= (uint32_t)o) incl += t;
-            }
-            uint32_t base = 0;
-            if (lane == 31 && incl) base = atomicAdd(&w.hit_n[par], incl);
-            base = __shfl_sync(0xffffffffu, base, 31) + incl - nh;
+            // this lane's hits: all loads first, then the actions
+            typename OnHit::State hs[kPerThread];
 #pragma unroll
-            for (uint32_t p = 0; p < kPerThread; p++) {
-                if (hitmask & (1u << p)) {
-                    w.hit_k[base] = (uint16_t)hk[p];
-                    w.hit_pos[base] = hp[p];
-                    w.hit_a[base] = ha[p];
-                    base++;
-                }
-            }
-            __syncthreads();
-            prof_mark(w, PF_PROBE);
-            // pass 2: up to kPerThread hits per thread; hit_load issues the
-            // loads of all of them before hit_apply acts on any
-            const uint32_t n = w.hit_n[par];
-            {
-                typename OnHit::State hs[kPerThread];
+            for (uint32_t p = 0; p < kPerThread; p++)
+                if (hitmask & (1u << p)) on_hit.load(hs[p], hk[p], hp[p], ha[p]);
 #pragma unroll
-                for (uint32_t q = 0; q < kPerThread; q++) {
-                    const uint32_t i = threadIdx.x + q * kThreads;
-                    if (i < n) on_hit.load(hs[q], w.hit_k[i], w.hit_pos[i], w.hit_a[i]);
-                }
-#pragma unroll
-                for (uint32_t q = 0; q < kPerThread; q++) {
-                    const uint32_t i = threadIdx.x + q * kThreads;
-                    if (i < n) on_hit.apply(hs[q]);
-                }
-            }
-            if (threadIdx.x == 0) w.hit_n[par ^ 1] = 0;
-            par ^= 1;
-            __syncthreads();
-            prof_mark(w, PF_HITS);
+            for (uint32_t p = 0; p < kPerThread; p++)
+                if (hitmask & (1u << p)) on_hit.apply(hs[p]);
         }
+        __syncthreads();
+        prof_mark(w, PF_PROBE);
         slice_done(cl, c0 + kSliceMids > s_hi);
         __syncthreads();
         prof_mark(w, PF_FLUSH);
     }
-    if (threadIdx.x == 0) w.hit_n[0] = w.hit_n[1] = 0;
-    __syncthreads();
 }
 
 // Row prefix of neighbour degrees (one warp per vertex): rowpre[off + s] =
