@@ -30,6 +30,24 @@ fixed time budget (20 s); edges peeled / elapsed time.  Peeling takes the
 cheapest edges first, so the sample overstates the CPU's whole-run rate.
 Warm-up steps of the reference arm compute the supports only.
 
+Batched workload (--workload batch<N>, e.g. batch256): the first N graphs of
+the 4,096-graph batch (gen.batch_graph: m log-uniform in [1e3, 2e6], Chung-Lu
+gamma 2.3, seed 4+i).  A step is one msp of all N graphs packed into one
+arena (bt_msp_batch layout) and peeled by one persistent launch; value =
+graphs per second of device time with the arena resident; e2e = the whole
+bt_msp_batch call from host graphs to host results.  The line also carries
+the per-graph loop of the plain engine on the same graphs (upload + bt_msp
+each), the schedule the autotuner picked, and a CPU sample (oracle, graphs in
+order for a fixed time budget).
+
+Serving workload (--workload serve): requests arrive as a Poisson stream at
+each rate of --rates; 95% of them name a graph of the batched workload's size
+distribution (the first --pool graphs of the batch), 5% a 10M-edge Chung-Lu
+graph (gamma 2.1); the op mix is 50% msp, 30% ebfc, 20% bfc.  A 4-slot
+bt_server with a 160 GB HBM budget serves them; the line reports graphs/s and
+p50/p99 latency per rate, the per-request loop of the plain engine on the
+same request list, and the isolated solve latency of each request.
+
 Multi-GPU: msp does not shard (every sub-round needs the global frontier), so
 N > 1 runs N independent replicas, one per rank ("replicas only").
 """
@@ -313,6 +331,234 @@ def run_ours(args):
     return 0
 
 
+def batch_graphs(workload: str):
+    from gpu_bitruss_gb300 import gen
+    import gpu_bitruss_gb300 as bt
+    count = int(workload[len("batch"):])
+    sizes = gen.batch_sizes()
+    lists = [gen.batch_graph(i, sizes=sizes) for i in range(count)]
+    graphs = [bt.Graph.from_edges(u, v) for u, v in lists]
+    return graphs, lists
+
+
+def run_batch(args):
+    import torch
+    import gpu_bitruss_gb300 as bt
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    t_gen = time.perf_counter()
+    graphs, lists = batch_graphs(args.workload)
+    t_gen = time.perf_counter() - t_gen
+    count = len(graphs)
+    edges = int(sum(g.m for g in graphs))
+    ctx = bt.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
+
+    # autotune the peel schedule on a sample arena (every 8th graph)
+    sample = graphs[::8]
+    arena_s, _ = bt.pack(sample)
+    ctx.upload(arena_s)
+    t_tune = time.perf_counter()
+    sched, tune_ms = ctx.autotune()
+    t_tune = time.perf_counter() - t_tune
+
+    # the arena resident in HBM
+    arena, base = bt.pack(graphs)
+    ctx.upload(arena)
+    for _ in range(args.warmup):
+        ctx.msp(out=False)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    total_ms, peel_ms = 0.0, []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        ctx.msp(out=False)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        peel_ms.append(ctx.phase_ms("peel"))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    stats = ctx.stats()
+    t_max = total_ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * count * args.steps / (t_max / 1000.0)
+
+    # e2e: host graphs -> bt_msp_batch -> host results
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res, levels = ctx.msp_batch(graphs)
+        e2e_ms += 1000 * (time.perf_counter() - t0)
+    h2d = sum(4 * (g.n + 1) + 4 * g.n + 16 * g.m for g in graphs)
+
+    # per-graph loop of the plain engine on the same graphs
+    loop_dev_ms, loop_wall = 0.0, time.perf_counter()
+    mismatch = 0
+    for i, g in enumerate(graphs):
+        ctx.upload(g)
+        b, _ = ctx.msp(out=True)
+        loop_dev_ms += ctx.phase_ms("msp")
+        mismatch += int(not np.array_equal(b, res[i]))
+    loop_wall = time.perf_counter() - loop_wall
+
+    line = {
+        "metric": "batched msp graphs/s", "value": value, "unit": "graphs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "uint64",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "graphs": count, "edges": edges,
+                   "desc": "first N graphs of the 4,096-graph batch: m log-uniform [1e3, 2e6], "
+                           "|U|:|V| uniform [0.2, 5], Chung-Lu gamma 2.3, seed 4+i",
+                   "arena": {"n": int(arena.n), "m": int(arena.m)}, "parallelism": "replicas",
+                   "l2": "512 MB flush between timed steps; arena > L2",
+                   "subrounds": stats[1], "levels": stats[0], "peel_ms": statistics.median(peel_ms),
+                   "schedule": {"min_grain": sched[0], "tasks_per_cta": sched[1], "local_plan": sched[2],
+                                "tuned_on": f"every 8th graph ({len(sample)} graphs, {int(arena_s.m)} edges)",
+                                "tune_s": round(t_tune, 2)},
+                   "gen_s": round(t_gen, 1)},
+        "e2e": {"value": world * count * args.steps / (e2e_ms / 1000.0), "unit": "graphs/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(4 * edges)},
+        "per_graph_loop": {"device_graphs_per_s": count / (loop_dev_ms / 1000.0),
+                           "e2e_graphs_per_s": count / loop_wall,
+                           "results_equal_batched": mismatch == 0},
+        "gpu_launches": 5 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        t0, done = time.perf_counter(), 0
+        for u, v in lists:
+            d = O.build_csr(u, v)
+            O.msp(d, os.cpu_count() or 1, O.MSP_TABLE)
+            done += 1
+            if time.perf_counter() - t0 > args.cpu_budget:
+                break
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": done / dt, "unit": "graphs/s", "cores": os.cpu_count() or 1,
+                                "kind": "port",
+                                "sample": f"oracle port msp, graphs in batch order for {args.cpu_budget:.0f} s "
+                                          f"({done} graphs in {dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_serve(args):
+    import threading
+    import torch
+    import gpu_bitruss_gb300 as bt
+    from gpu_bitruss_gb300 import gen
+
+    torch.cuda.set_device(0)
+    sizes = gen.batch_sizes()
+    t_gen = time.perf_counter()
+    pool = [bt.Graph.from_edges(*gen.batch_graph(i, sizes=sizes)) for i in range(args.pool)]
+    big = bt.Graph.from_edges(*gen.by_name("cl10000k"))
+    t_gen = time.perf_counter() - t_gen
+    rng = np.random.default_rng(5)
+    nreq = args.requests
+    reqs = []
+    for _ in range(nreq):
+        g = big if rng.random() < 0.05 else pool[int(rng.integers(0, len(pool)))]
+        x = rng.random()
+        op = "msp" if x < 0.5 else ("ebfc" if x < 0.8 else "bfc")
+        reqs.append((g, op))
+
+    # isolated solve of every request (one slot, nothing else in flight) and
+    # the per-request loop of the plain engine (upload + op + result, in turn)
+    srv = bt.Server(0, 1, 160 << 30)
+    for g, op in reqs[:4]:  # warm-up
+        srv.wait(srv.submit(g, op)[0])
+    iso = []
+    for g, op in reqs:
+        iso.append(srv.wait(srv.submit(g, op)[0])["total_ms"])
+    srv.close()
+    ctx = bt.Context(0)
+    t0 = time.perf_counter()
+    for g, op in reqs:
+        ctx.upload(g)
+        {"msp": ctx.msp, "ebfc": ctx.ebfc, "bfc": ctx.bfc}[op]()
+    loop_s = time.perf_counter() - t0
+    ctx.close()
+
+    per_rate = []
+    for rate in [float(r) for r in args.rates.split(",")]:
+        srv = bt.Server(0, args.slots, 160 << 30)
+        gaps = rng.exponential(1.0 / rate, size=nreq)
+        arrivals = np.cumsum(gaps)
+        tickets = [None] * nreq
+        start = time.perf_counter()
+
+        def feed():
+            for i, (g, op) in enumerate(reqs):
+                dt = start + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                tickets[i] = srv.submit(g, op)[0]
+
+        th = threading.Thread(target=feed)
+        th.start()
+        lat, batched = [], 0
+        for i in range(nreq):
+            while tickets[i] is None:
+                time.sleep(0.0005)
+            info = srv.wait(tickets[i])
+            lat.append(info["total_ms"])
+            batched += info["batch_size"] > 1
+        end = time.perf_counter()
+        th.join()
+        st = srv.stats()
+        srv.close()
+        lat = np.array(lat)
+        per_rate.append({"rate_req_s": rate, "graphs_per_s": nreq / (end - start),
+                         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                         "batched_requests": int(batched), "batches": int(st["batches"])})
+    iso = np.array(iso)
+    best = max(per_rate, key=lambda r: r["graphs_per_s"])
+    line = {
+        "metric": "served graphs/s", "value": best["graphs_per_s"], "unit": "graphs/s", "n_gpus": 1,
+        "steps": len(per_rate), "warmup": 4, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "uint64", "data": "synthetic",
+        "config": {"workload": "serve", "requests": nreq, "slots": args.slots, "hbm_budget_gb": 160,
+                   "pool": f"first {args.pool} graphs of the batch (m log-uniform [1e3, 2e6]) + one "
+                           f"10M-edge Chung-Lu gamma 2.1 graph at 5%",
+                   "ops": "50% msp, 30% ebfc, 20% bfc", "gen_s": round(t_gen, 1)},
+        "per_rate": per_rate,
+        "isolated_solve_ms": {"p50": float(np.percentile(iso, 50)), "p99": float(np.percentile(iso, 99))},
+        "per_request_loop": {"graphs_per_s": nreq / loop_s},
+        "e2e": {"value": best["graphs_per_s"], "unit": "graphs/s",
+                "h2d_bytes_per_step": int(sum(4 * (g.n + 1) + 4 * g.n + 16 * g.m for g, _ in reqs)),
+                "d2h_bytes_per_step": int(sum((4 if op == "msp" else 8 if op == "ebfc" else 0) * g.m
+                                              for g, op in reqs))},
+        "gpu_launches": None,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -324,9 +570,17 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of CPU peeling per sample step")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rates", default="100,1000,5000", help="serve: request rates (req/s)")
+    ap.add_argument("--requests", type=int, default=200, help="serve: requests per rate")
+    ap.add_argument("--pool", type=int, default=96, help="serve: graphs of the batch distribution")
+    ap.add_argument("--slots", type=int, default=4, help="serve: server slots")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload.startswith("batch"):
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

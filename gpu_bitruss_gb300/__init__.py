@@ -27,6 +27,7 @@ import numpy as np
 __all__ = [
     "BitrussError", "Graph", "Context", "load", "build",
     "bfc_vpp", "bfc_evpp", "g_bitruss_hindex", "bitruss_msp", "bitruss_msp_exact", "bfc_noalloc",
+    "pack", "Server", "OPS",
     "STATUS", "SYMBOLS",
 ]
 
@@ -48,7 +49,13 @@ SYMBOLS = [
     "bt_bfc", "bt_ebfc", "bt_hidx", "bt_msp", "bt_msp_exact", "bt_result_download",
     "bt_ctx_phase_ms", "bt_ctx_stats", "bt_status_string", "bt_last_error",
     "bt_bfc_noalloc",
+    "bt_ctx_set_msp_schedule", "bt_ctx_get_msp_schedule", "bt_msp_autotune",
+    "bt_graph_pack", "bt_ctx_set_arena_edges", "bt_msp_batch", "bt_ebfc_batch",
+    "bt_ctx_memory_peak", "bt_server_create", "bt_server_submit", "bt_server_wait",
+    "bt_server_latency", "bt_server_stats", "bt_server_free", "bt_job_bytes",
 ]
+
+OPS = {"bfc": 0, "ebfc": 1, "msp": 2, "msp_exact": 3}
 
 
 class BitrussError(RuntimeError):
@@ -64,6 +71,14 @@ class _View(C.Structure):
         ("m", C.c_uint64), ("support_max", C.c_uint64),
         ("offsets", C.c_void_p), ("neighbors", C.c_void_p), ("degrees", C.c_void_p),
         ("edges", C.c_void_p), ("edge_ids", C.c_void_p),
+    ]
+
+
+class _RequestInfo(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("count", C.c_uint64), ("support_max", C.c_uint64),
+        ("levels", C.c_uint32), ("batch_size", C.c_uint32),
+        ("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
     ]
 
 
@@ -109,6 +124,21 @@ def load():
         "bt_status_string": ([i32], C.c_char_p),
         "bt_last_error": ([], C.c_char_p),
         "bt_bfc_noalloc": ([i32, P, P, u32, u64, P, P], i32),
+        "bt_ctx_set_msp_schedule": ([P, u32, u32, u32], i32),
+        "bt_ctx_get_msp_schedule": ([P, P], i32),
+        "bt_msp_autotune": ([P, P, C.POINTER(C.c_double)], i32),
+        "bt_graph_pack": ([P, u32, C.POINTER(P), P], i32),
+        "bt_ctx_set_arena_edges": ([P, u64], i32),
+        "bt_msp_batch": ([P, P, u32, i32, P, P], i32),
+        "bt_ebfc_batch": ([P, P, u32, P, P], i32),
+        "bt_ctx_memory_peak": ([P, C.POINTER(u64), i32], i32),
+        "bt_server_create": ([i32, u32, u64, C.POINTER(P)], i32),
+        "bt_server_submit": ([P, P, i32, P, C.POINTER(u64)], i32),
+        "bt_server_wait": ([P, u64, C.c_double, C.POINTER(_RequestInfo)], i32),
+        "bt_server_latency": ([P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64), i32], i32),
+        "bt_server_stats": ([P, C.POINTER(u64), i32], i32),
+        "bt_server_free": ([P], None),
+        "bt_job_bytes": ([P, P, u32, i32, C.POINTER(u64)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -222,6 +252,18 @@ class Context:
         _check(load().bt_ctx_memory_used(self._c, C.byref(x)), "memory_used")
         return x.value
 
+    def memory_peak(self, reset: bool = False) -> int:
+        x = C.c_uint64()
+        _check(load().bt_ctx_memory_peak(self._c, C.byref(x), 1 if reset else 0), "memory_peak")
+        return x.value
+
+    def job_bytes(self, graphs: list, op: str) -> int:
+        """The server's admission estimate for one arena of `graphs` and `op`."""
+        hs, _ = _handles(graphs)
+        x = C.c_uint64()
+        _check(load().bt_job_bytes(self._c, hs, len(graphs), OPS[op], C.byref(x)), "job_bytes")
+        return x.value
+
     def upload(self, g: Graph) -> None:
         _check(load().bt_graph_upload(self._c, g._h), "graph upload")
         self.graph = g
@@ -253,6 +295,46 @@ class Context:
         _check(f(self._c, _ptr(b) if m else None, C.byref(lv)), "bitruss_msp")
         return b, lv.value
 
+    # schedule and autotuner ------------------------------------------------
+    def set_msp_schedule(self, min_grain: int = 0, tasks_per_cta: int = 0, local_plan: int = 0) -> None:
+        _check(load().bt_ctx_set_msp_schedule(self._c, min_grain, tasks_per_cta, local_plan),
+               "set_msp_schedule")
+
+    def msp_schedule(self) -> tuple[int, int, int]:
+        a = np.zeros(3, np.uint32)
+        _check(load().bt_ctx_get_msp_schedule(self._c, _ptr(a)), "msp_schedule")
+        return tuple(int(x) for x in a)
+
+    def autotune(self) -> tuple[tuple[int, int, int], float]:
+        """Tune the msp schedule on the resident graph; returns (schedule, kernel ms)."""
+        a = np.zeros(3, np.uint32)
+        ms = C.c_double()
+        _check(load().bt_msp_autotune(self._c, _ptr(a), C.byref(ms)), "msp autotune")
+        return tuple(int(x) for x in a), ms.value
+
+    # batched arenas ----------------------------------------------------------
+    def set_arena_edges(self, edges: int) -> None:
+        _check(load().bt_ctx_set_arena_edges(self._c, edges), "set_arena_edges")
+
+    def msp_batch(self, graphs: list, exact: bool = False):
+        """Bitruss numbers of every graph (one array each) and their level counts."""
+        hs, base = _handles(graphs)
+        b = np.zeros(max(int(base[-1]), 1), np.uint32)
+        lv = np.zeros(max(len(graphs), 1), np.uint32)
+        _check(load().bt_msp_batch(self._c, hs, len(graphs), 1 if exact else 0, _ptr(b), _ptr(lv)),
+               "msp batch")
+        self.graph = None  # the context now holds the last arena
+        return [b[base[i]:base[i + 1]] for i in range(len(graphs))], lv[:len(graphs)]
+
+    def ebfc_batch(self, graphs: list):
+        """Supports of every graph (one array each) and their butterfly counts."""
+        hs, base = _handles(graphs)
+        sup = np.zeros(max(int(base[-1]), 1), np.uint64)
+        cnt = np.zeros(max(len(graphs), 1), np.uint64)
+        _check(load().bt_ebfc_batch(self._c, hs, len(graphs), _ptr(sup), _ptr(cnt)), "ebfc batch")
+        self.graph = None
+        return [sup[base[i]:base[i + 1]] for i in range(len(graphs))], cnt[:len(graphs)]
+
     def download(self, out: np.ndarray) -> None:
         _check(load().bt_result_download(self._c, _ptr(out), out.nbytes), "result download")
 
@@ -280,6 +362,74 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Request loop (bt_server_*): submit graphs with an op, wait for tickets."""
+
+    def __init__(self, device: int = 0, slots: int = 2, hbm_budget: int = 0):
+        self._s = C.c_void_p()
+        _check(load().bt_server_create(device, slots, hbm_budget, C.byref(self._s)), "bt_server_create")
+        self._keep = {}
+
+    def submit(self, g: Graph, op: str):
+        """Queue a request; returns (ticket, output array or None)."""
+        out = None
+        if op in ("msp", "msp_exact"):
+            out = np.zeros(max(g.m, 1), np.uint32)
+        elif op == "ebfc":
+            out = np.zeros(max(g.m, 1), np.uint64)
+        t = C.c_uint64()
+        _check(load().bt_server_submit(self._s, g._h, OPS[op], _ptr(out), C.byref(t)), "server submit")
+        self._keep[t.value] = (g, out)
+        return t.value, (out[:g.m] if out is not None else None)
+
+    def wait(self, ticket: int, timeout_ms: float = -1.0) -> dict:
+        info = _RequestInfo()
+        rc = load().bt_server_wait(self._s, ticket, timeout_ms, C.byref(info))
+        if rc != 7:  # BT_ERR_TIMEOUT keeps the ticket
+            self._keep.pop(ticket, None)
+        _check(rc, "server wait")
+        return {k: getattr(info, k) for k, _ in _RequestInfo._fields_}
+
+    def latency(self, reset: bool = False) -> tuple[float, float, int]:
+        p50, p99, n = C.c_double(), C.c_double(), C.c_uint64()
+        _check(load().bt_server_latency(self._s, C.byref(p50), C.byref(p99), C.byref(n), 1 if reset else 0),
+               "server latency")
+        return p50.value, p99.value, n.value
+
+    def stats(self) -> dict:
+        a = (C.c_uint64 * 6)()
+        _check(load().bt_server_stats(self._s, a, 6), "server stats")
+        return dict(zip(["budget", "reserved", "running", "queued", "batches", "batched_requests"], list(a)))
+
+    def close(self):
+        if getattr(self, "_s", None):
+            load().bt_server_free(self._s)
+            self._s = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _handles(graphs: list):
+    arr = (C.c_void_p * max(len(graphs), 1))(*[g._h for g in graphs])
+    base = np.zeros(len(graphs) + 1, np.int64)
+    base[1:] = np.cumsum([g.m for g in graphs]) if graphs else []
+    return arr, base
+
+
+def pack(graphs: list) -> tuple["Graph", np.ndarray]:
+    """The arena of a batched call as a host graph, with each graph's first edge id."""
+    hs, _ = _handles(graphs)
+    base = np.zeros(len(graphs) + 1, np.uint64)
+    h = C.c_void_p()
+    _check(load().bt_graph_pack(hs, len(graphs), C.byref(h), _ptr(base)), "graph pack")
+    return Graph(h), base
 
 
 _default_ctx: Context | None = None

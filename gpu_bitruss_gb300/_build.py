@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, "libbitruss.so")
 COH = os.path.join(PKG, "coh")
 
 CUDA_SOURCES = ["bt_ctx.cu", "bt_count.cu", "bt_msp.cu", "bt_hidx.cu", "bt_noalloc.cu"]
-CXX_SOURCES = ["bt_graph.cpp"]
+CXX_SOURCES = ["bt_graph.cpp", "bt_batch.cpp", "bt_server.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

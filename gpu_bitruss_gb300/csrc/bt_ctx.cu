@@ -59,6 +59,25 @@ extern "C" const char *bt_status_string(bt_status s) {
 // device arena
 // ---------------------------------------------------------------------------
 
+// Device memory comes from the device's stream-ordered pool
+// (cudaMallocAsync / cudaFreeAsync on the context's stream): no device-wide
+// synchronisation per allocation or free, so contexts on different streams
+// (the serving slots) overlap, and freed blocks are reused from the pool.
+namespace {
+std::once_flag g_pool_once[64];
+
+void pool_setup(int device) {
+    if (device < 0 || device >= 64) return;
+    std::call_once(g_pool_once[device], [device]() {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = 8ull << 30;  // keep up to 8 GiB of freed blocks for reuse
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    });
+}
+}  // namespace
+
 bt_status ctx_alloc(bt_ctx *ctx, void **p, uint64_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
@@ -67,12 +86,14 @@ bt_status ctx_alloc(bt_ctx *ctx, void **p, uint64_t bytes) {
         return bt_fail(BT_ERR_DEVICE_MEMORY, "device budget of " + std::to_string(ctx->budget) +
                                                  " bytes exceeded (need " +
                                                  std::to_string(ctx->used + bytes) + ")");
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = cudaMallocAsync(p, bytes, ctx->stream);
     if (e != cudaSuccess) {
         *p = nullptr;
-        return bt_cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+        cudaGetLastError();
+        return bt_cuda_fail(e, "cudaMallocAsync", __FILE__, __LINE__);
     }
     ctx->used += bytes;
+    if (ctx->used > ctx->peak) ctx->peak = ctx->used;
     ctx->allocs.emplace_back(*p, bytes);
     return BT_OK;
 }
@@ -86,7 +107,7 @@ void ctx_free(bt_ctx *ctx, void *p) {
             break;
         }
     }
-    cudaFree(p);
+    cudaFreeAsync(p, ctx->stream);
 }
 
 bt_status ctx_scratch(bt_ctx *ctx, uint64_t bytes, void **p) {
@@ -112,6 +133,7 @@ void ctx_release_graph(bt_ctx *ctx) {
     ctx_free(ctx, g.hub_base);
     ctx_free(ctx, g.hub_mask);
     ctx_free(ctx, g.hub_pool);
+    ctx_free(ctx, g.seg_base);
     ctx_free(ctx, ctx->sup);
     ctx_free(ctx, ctx->result);
     ctx->sup = nullptr;
@@ -152,6 +174,7 @@ extern "C" bt_status bt_ctx_create(int device, bt_ctx **out) {
     }
     ctx->stream = ctx->own_stream;
     for (auto &ev : ctx->ev) cudaEventCreate(&ev);
+    pool_setup(device);
     *out = ctx;
     return BT_OK;
 }
@@ -174,11 +197,21 @@ extern "C" bt_status bt_ctx_memory_used(const bt_ctx *ctx, uint64_t *bytes) {
     return BT_OK;
 }
 
+extern "C" bt_status bt_ctx_memory_peak(bt_ctx *ctx, uint64_t *bytes, int reset) {
+    if (!ctx || !bytes) return bt_fail(BT_ERR_INVALID, "null argument");
+    *bytes = ctx->peak;
+    if (reset) ctx->peak = ctx->used;
+    return BT_OK;
+}
+
 extern "C" void bt_ctx_free(bt_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    // free in the context's own stream order (a caller's stream may be gone by now)
+    ctx->stream = ctx->own_stream;
     while (!ctx->allocs.empty()) ctx_free(ctx, ctx->allocs.back().first);
+    cudaStreamSynchronize(ctx->own_stream);
     for (auto &ev : ctx->ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -259,6 +292,26 @@ __global__ void k_hub_sizes(uint32_t n, const uint32_t *deg, uint32_t *size, uin
 
 __global__ void k_hub_build(bt::Rows r, uint32_t n, uint2 *pool) { bt::hub_build(r, n, pool); }
 
+// batched arena: graph index of each vertex in priority order
+__global__ void k_gather_seg(uint32_t n, const uint32_t *order, const uint32_t *seg, uint32_t *seg_r) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        seg_r[i] = seg[order[i]];
+}
+
+// first rank of each rank's graph (ranks grouped by graph, graph index ascending)
+__global__ void k_seg_base(uint32_t n, const uint32_t *seg_sorted, uint32_t *base) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = seg_sorted[i];
+        uint32_t lo = 0, hi = i;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (seg_sorted[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        base[i] = lo;
+    }
+}
+
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned cap) {
     uint64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;
@@ -294,14 +347,17 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
     // staging: reference CSR on device (freed at the end)
     uint32_t *s_off = nullptr, *s_nbr = nullptr, *s_eid = nullptr, *s_deg = nullptr;
     uint32_t *rank = nullptr, *order = nullptr, *vals = nullptr, *t_nbr = nullptr, *t_eid = nullptr;
+    uint32_t *s_seg = nullptr, *seg_r = nullptr, *seg_r2 = nullptr, *order2 = nullptr;
     unsigned long long *keys = nullptr, *keys2 = nullptr;
     void *temp = nullptr;
     bt_status rc = BT_OK;
+    const bool segmented = !hg->segment.empty();
     auto cleanup = [&]() {
         ctx_free(ctx, s_off); ctx_free(ctx, s_nbr); ctx_free(ctx, s_eid); ctx_free(ctx, s_deg);
         ctx_free(ctx, rank); ctx_free(ctx, order); ctx_free(ctx, vals);
         ctx_free(ctx, t_nbr); ctx_free(ctx, t_eid);
         ctx_free(ctx, keys); ctx_free(ctx, keys2); ctx_free(ctx, temp);
+        ctx_free(ctx, s_seg); ctx_free(ctx, seg_r); ctx_free(ctx, seg_r2); ctx_free(ctx, order2);
     };
 #define STEP(x)                 \
     do {                        \
@@ -347,12 +403,42 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
                                               (int64_t)n, g.off, g.off + 1, st));
     size_t tb = t1 > t2 ? t1 : t2;
     tb = tb > t3 ? tb : t3;
+    int seg_bits = 1;
+    if (segmented) {
+        if (hg->segment.size() != n) {
+            cleanup();
+            return bt_fail(BT_ERR_INVALID, "arena segment array does not match the vertex count");
+        }
+        uint32_t maxseg = 0;
+        for (uint32_t x : hg->segment) maxseg = x > maxseg ? x : maxseg;
+        while (seg_bits < 32 && (maxseg >> seg_bits)) seg_bits++;
+        STEP(ctx_alloc_t(ctx, &s_seg, n));
+        STEP(ctx_alloc_t(ctx, &seg_r, n));
+        STEP(ctx_alloc_t(ctx, &seg_r2, n));
+        STEP(ctx_alloc_t(ctx, &order2, n));
+        STEP(ctx_alloc_t(ctx, &g.seg_base, n));
+        STEPC(cudaMemcpyAsync(s_seg, hg->segment.data(), 4ull * n, cudaMemcpyHostToDevice, st));
+        size_t t5 = 0;
+        STEPC(cub::DeviceRadixSort::SortPairs(nullptr, t5, seg_r, seg_r2, order, order2, (int)n, 0, seg_bits, st));
+        tb = tb > t5 ? tb : t5;
+    }
+    g.cnt_span = segmented ? hg->seg_max_n : n;
     STEP(ctx_alloc(ctx, &temp, tb));
 
     unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (n) {
         k_rank_keys<<<grid_for(n, blk, cap), blk, 0, st>>>(n, s_deg, keys, vals);
         STEPC(cub::DeviceRadixSort::SortPairs(temp, t1, keys, keys2, vals, order, (int)n, 0, 64, st));
+        if (segmented) {
+            // group the ranks by graph, priority order kept within a graph (stable sort)
+            k_gather_seg<<<grid_for(n, blk, cap), blk, 0, st>>>(n, order, s_seg, seg_r);
+            size_t t5 = tb;
+            STEPC(cub::DeviceRadixSort::SortPairs(temp, t5, seg_r, seg_r2, order, order2, (int)n, 0, seg_bits,
+                                                  st));
+            std::swap(order, order2);
+            k_seg_base<<<grid_for(n, blk, cap), blk, 0, st>>>(n, seg_r2, g.seg_base);
+            STEPC(cudaGetLastError());
+        }
         k_rank_scatter<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.u_num, order, s_deg, rank, g.deg0, g.is_u);
     }
     // off = exclusive scan of deg0 over n+1 entries (deg0[n] read as garbage is

@@ -44,6 +44,10 @@ struct bt_graph {
     std::vector<uint32_t> edge_ids;   // 2m
     std::vector<uint32_t> edge_support_raw;  // m, as stored in a .bin (int32 bits)
     std::vector<uint32_t> bitruss_raw;       // m, as stored in a .bin
+    // batched arena only: graph index of every vertex (empty for one graph)
+    // and the vertex count of the largest graph
+    std::vector<uint32_t> segment;
+    uint32_t seg_max_n = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -72,6 +76,10 @@ struct DevGraph {
     uint32_t *hub_mask = nullptr;
     uint2 *hub_pool = nullptr;
     uint64_t hub_slots = 0;
+    // batched arena: ranks are grouped by graph; seg_base[r] = first rank of
+    // r's graph (NULL for one graph); cnt_span = vertices of the largest graph
+    uint32_t *seg_base = nullptr;
+    uint32_t cnt_span = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -85,6 +93,7 @@ struct bt_ctx {
     cudaStream_t stream = nullptr;
     uint64_t budget = 0;       // 0 = unlimited
     uint64_t used = 0;
+    uint64_t peak = 0;         // high-water mark of `used`
     std::vector<std::pair<void *, uint64_t>> allocs;
 
     DevGraph g;
@@ -106,6 +115,10 @@ struct bt_ctx {
     uint64_t work[12] = {0};  // msp work counters and phase times of the last call
     uint64_t prof[8] = {0};   // msp: SM cycles per CTA by step (task, stage, slice, probe, hits, flush, barrier, other)
     cudaEvent_t ev[8] = {};
+
+    // msp task schedule (0 = built-in value): min grain, tasks per CTA, local-plan limit
+    uint32_t msp_schedule[3] = {0, 0, 0};
+    uint64_t arena_edges = 1ull << 28;  // batched calls: edges per arena, at most
 };
 
 enum { PH_UPLOAD = 0, PH_EBFC = 1, PH_PEEL = 2, PH_HIDX = 3, PH_TOTAL = 4, PH_MSP = 5 };

@@ -46,6 +46,7 @@
 // the kernel returns.
 #include <cstdio>
 #include <cstdlib>
+#include <mutex>
 
 #include "bt_device.cuh"
 #include "bt_internal.h"
@@ -54,8 +55,9 @@ namespace {
 
 using bt::kEmpty;
 using bt::kThreads;
-constexpr uint32_t kMinGrain = 2048;    // plain probe positions per task, at least
-constexpr uint32_t kLocalPlan = 512;    // frontiers up to this size are planned by every CTA
+constexpr uint32_t kMinGrain = 2048;    // default: plain probe positions per task, at least
+constexpr uint32_t kTasksPerCta = 2;    // default: tasks per CTA a sub-round's work is cut into
+constexpr uint32_t kLocalPlan = 512;    // frontiers up to this size may be planned by every CTA
 
 struct MspState {
     bt::Barrier bar;
@@ -94,6 +96,7 @@ struct TraceRow {
 struct MspArgs {
     MspState *s;
     uint32_t n, nblocks, exact;
+    uint32_t min_grain, tasks_per_cta, local_plan;  // task schedule (results do not depend on it)
     uint64_t m;
     unsigned long long wait_ns;
     const uint32_t *off;
@@ -207,10 +210,10 @@ __device__ __forceinline__ bool barrier(const MspArgs &a, Smem &sm) {
 // ---------------------------------------------------------------------------
 //
 // The pivot is the endpoint whose row's probe total (two_hop) is smaller.  The
-// grain is the sub-round's total over two tasks per CTA (tasks are taken
-// dynamically, so two per CTA even out their unequal real costs), at least
-// kMinGrain and, for an anchor staged in shared memory, at least twice its
-// row (each task stages that row).
+// grain is the sub-round's total over tasks_per_cta tasks per CTA (tasks are
+// taken dynamically, so a few per CTA even out their unequal real costs), at
+// least min_grain and, for an anchor staged in shared memory, at least twice
+// its row (each task stages that row).
 // Writes piv/anc per edge, the grain (bit 31: the pivot is the V end), the
 // pivot row's probe total and the exclusive prefix of task counts
 // (start[len] = number of tasks).  Runs on one whole CTA.
@@ -237,8 +240,8 @@ __device__ void plan(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t 
     for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
     if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&sm.total, mine);
     __syncthreads();
-    unsigned long long g = sm.total / (2ull * a.nblocks);
-    if (g < kMinGrain) g = kMinGrain;
+    unsigned long long g = sm.total / ((unsigned long long)a.tasks_per_cta * a.nblocks);
+    if (g < a.min_grain) g = a.min_grain;
     if (g > (1u << 30)) g = 1u << 30;
     unsigned long long anchor = 0;
     for (uint32_t base = 0; base < len; base += kThreads) {
@@ -573,7 +576,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
         rd.near_list = a.near_a;
         rd.near_len = &s->near_ctr[nsel];
         uint32_t ntasks;
-        if (curr_len <= kLocalPlan) {
+        if (curr_len <= a.local_plan) {
             plan(a, sm, curr, curr_len, sm.lp_piv, sm.lp_anc, sm.lp_grain, sm.lp_total, sm.lp_start,
                  blockIdx.x == 0);
             ntasks = sm.lp_start[curr_len];
@@ -598,7 +601,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
             s->edge_num -= curr_len;
             s->subrounds++;
         }
-        if (curr_len <= kLocalPlan)
+        if (curr_len <= a.local_plan)
             peel_tasks(a, sm, curr, curr_len, sm.lp_piv, sm.lp_anc, sm.lp_grain, sm.lp_total, sm.lp_start,
                        ntasks, &s->task_ctr[r % 3], rd, epoch, wk);
         else
@@ -656,6 +659,8 @@ __global__ void k_msp_init(uint64_t m, const unsigned long long *sup_in, unsigne
 __global__ void k_two_hop(MspArgs a) { compute_two_hop(a); }
 
 }  // namespace
+
+static std::mutex g_coop_mutex;
 
 static unsigned long long wait_limit_ns() {
     const char *us = getenv("BT_WAIT_LIMIT_US");
@@ -744,6 +749,9 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     a.n = g.n;
     a.m = m;
     a.exact = exact ? 1u : 0u;
+    a.min_grain = ctx->msp_schedule[0] ? ctx->msp_schedule[0] : kMinGrain;
+    a.tasks_per_cta = ctx->msp_schedule[1] ? ctx->msp_schedule[1] : kTasksPerCta;
+    a.local_plan = ctx->msp_schedule[2] ? std::min(ctx->msp_schedule[2], kLocalPlan) : kLocalPlan;
     a.wait_ns = wait_limit_ns();
     a.off = g.off;
     a.ends = g.ends;
@@ -757,12 +765,12 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
         C(cudaGetLastError());
     }
     // edge_num = live edges
+    MspState h0;
     {
+        C(cudaMemcpyAsync(&h0, s, sizeof(MspState), cudaMemcpyDeviceToHost, st));
         C(cudaStreamSynchronize(st));
-        MspState h;
-        C(cudaMemcpy(&h, s, sizeof(MspState), cudaMemcpyDeviceToHost));
-        h.edge_num = h.far_len;
-        C(cudaMemcpy(s, &h, sizeof(MspState), cudaMemcpyHostToDevice));
+        h0.edge_num = h0.far_len;
+        C(cudaMemcpyAsync(s, &h0, sizeof(MspState), cudaMemcpyHostToDevice, st));
     }
     if (n) {
         k_two_hop<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(a);
@@ -775,22 +783,41 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     C(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msp, kThreads, smem));
     if (per_sm < 1) { release(); return bt_fail(BT_ERR_CUDA, "msp kernel does not fit on an SM"); }
     a.nblocks = (uint32_t)(ctx->sm_count * per_sm);
+    // One cooperative peeling kernel at a time in this process: two grids that
+    // each fill the GPU could both be partly resident, each waiting at its
+    // grid barrier for CTAs that cannot be placed.  Contexts on other streams
+    // (serving slots) still overlap their counting, uploads and copies.
+    std::unique_lock<std::mutex> coop(g_coop_mutex, std::defer_lock);
     if (m) {
+        coop.lock();
         void *params[] = {&a};
         cudaEventRecord(ctx->ev[4], st);
-        C(cudaLaunchCooperativeKernel((void *)k_msp, dim3(a.nblocks), dim3(kThreads), params, smem, st));
-        C(cudaGetLastError());
+        cudaError_t le = cudaLaunchCooperativeKernel((void *)k_msp, dim3(a.nblocks), dim3(kThreads), params, smem, st);
+        if (le == cudaSuccess) le = cudaGetLastError();
+        if (le != cudaSuccess) {
+            coop.unlock();
+            release();
+            return bt_cuda_fail(le, "cudaLaunchCooperativeKernel(k_msp)", __FILE__, __LINE__);
+        }
         cudaEventRecord(ctx->ev[5], st);
     }
     cudaEventRecord(e1, st);
     MspState h{};
-    C(cudaMemcpyAsync(&h, s, sizeof(MspState), cudaMemcpyDeviceToHost, st));
-    C(cudaStreamSynchronize(st));
+    {
+        cudaError_t ce = cudaMemcpyAsync(&h, s, sizeof(MspState), cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (coop.owns_lock()) coop.unlock();
+        if (ce != cudaSuccess) {
+            release();
+            return bt_cuda_fail(ce, "msp state readback", __FILE__, __LINE__);
+        }
+    }
     if (a.trace) {
         // rows 2 .. subrounds+1 are sub-rounds; written as raw TraceRow records
         const uint64_t rows = std::min<uint64_t>(h.subrounds + 2, a.trace_cap);
         std::vector<TraceRow> tr(rows);
-        C(cudaMemcpy(tr.data(), a.trace, sizeof(TraceRow) * rows, cudaMemcpyDeviceToHost));
+        C(cudaMemcpyAsync(tr.data(), a.trace, sizeof(TraceRow) * rows, cudaMemcpyDeviceToHost, st));
+        C(cudaStreamSynchronize(st));
         if (FILE *f = fopen(trace_path, "wb")) {
             fwrite(tr.data(), sizeof(TraceRow), rows, f);
             fclose(f);

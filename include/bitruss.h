@@ -95,6 +95,9 @@ bt_status bt_ctx_set_stream(bt_ctx *ctx, void *cuda_stream);
  * Allocations beyond it fail with BT_ERR_DEVICE_MEMORY. */
 bt_status bt_ctx_set_memory_budget(bt_ctx *ctx, uint64_t bytes);
 bt_status bt_ctx_memory_used(const bt_ctx *ctx, uint64_t *bytes);
+/* High-water mark of the bytes this context held since it was created or the
+ * mark was last reset (reset != 0 sets it to the current use after reading). */
+bt_status bt_ctx_memory_peak(bt_ctx *ctx, uint64_t *bytes, int reset);
 
 void bt_ctx_free(bt_ctx *ctx);
 
@@ -146,8 +149,124 @@ double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
  * [14..16] nanoseconds the peeling kernel spent in level transitions, peel
  * phases and finalize phases; [20..27] SM cycles per CTA of the peeling
  * kernel by step: task lookup, anchor staging, slice load, probe pass, hit
- * pass, flushes, grid-barrier waits, other work. */
+ * pass, flushes, grid-barrier waits, other work.  After a batched call, [1] is
+ * the sub-rounds summed over its arenas and [7] the number of arenas. */
 bt_status bt_ctx_stats(const bt_ctx *ctx, uint64_t *out, int n);
+
+/* ---- peeling schedule and its autotuner ------------------------------- */
+
+/* The msp task schedule.  min_grain: probe positions per peel task, at least;
+ * tasks_per_cta: a sub-round's work is cut into about this many tasks per
+ * CTA; local_plan: frontiers of at most this many edges (<= 512) are planned
+ * by every CTA without a grid barrier.  0 keeps the built-in value (2048, 2,
+ * 512).  Results never depend on the schedule.  No reference counterpart (the
+ * reference launches one block per frontier edge: bitruss_msp.cu:286-291). */
+bt_status bt_ctx_set_msp_schedule(bt_ctx *ctx, uint32_t min_grain, uint32_t tasks_per_cta,
+                                  uint32_t local_plan);
+/* out: 3 entries, the schedule in effect (built-in values filled in). */
+bt_status bt_ctx_get_msp_schedule(const bt_ctx *ctx, uint32_t *out);
+
+/* Autotuner: times the peeling kernel of bt_msp on the resident graph under
+ * candidate schedules (coordinate descent from the current one over short
+ * candidate lists), keeps the fastest on the context and returns it in out
+ * (3 entries, may be NULL) with its kernel time in *best_ms (may be NULL).
+ * Costs about ten msp runs of the resident graph: tune on a sample. */
+bt_status bt_msp_autotune(bt_ctx *ctx, uint32_t *out, double *best_ms);
+
+/* ---- batched arenas ---------------------------------------------------- */
+/*
+ * No reference counterpart: the reference decomposes one Graph per process
+ * (main.cu:91-128).  A batched call packs several graphs into one device
+ * arena -- their disjoint union, numbered as process_graph
+ * (src/graph/graph.cpp:74-242) numbers the concatenation of their edge lists:
+ * the U vertices of graph 0, 1, ... first, then their V vertices, and graph
+ * i's edge ids offset by the edge counts of graphs 0..i-1 -- and decomposes it
+ * with one persistent launch.  A butterfly never spans two graphs, so every
+ * graph's result equals the single-graph call on that graph (bit-exact).
+ * Graphs are cut, in the order given, into arenas of at most
+ * bt_ctx_set_arena_edges edges (default 2^28; a larger graph gets an arena of
+ * its own).  The last arena stays resident on the context afterwards.
+ */
+
+/* Pack `count` graphs into one host graph (the arena layout above).
+ * edge_base: count+1 entries (may be NULL), graph i's first edge id. */
+bt_status bt_graph_pack(const bt_graph *const *graphs, uint32_t count, bt_graph **out,
+                        uint64_t *edge_base);
+
+/* Largest arena, in edges, of this context's batched calls (1 .. 2^31-1). */
+bt_status bt_ctx_set_arena_edges(bt_ctx *ctx, uint64_t edges);
+
+/* msp (exact = 0, the reference rule) or the corrected rule (exact = 1) of
+ * every graph.  bitruss: sum of m entries, graph i's edges from edge_base[i]
+ * on in its own edge-id order; levels: count entries, each graph's "msp with
+ * N levels" figure.  Either may be NULL. */
+bt_status bt_msp_batch(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t count, int exact,
+                       uint32_t *bitruss, uint32_t *levels);
+
+/* Supports (sum of m entries, laid out as in bt_msp_batch) and butterfly
+ * counts (count entries) of every graph.  Either may be NULL. */
+bt_status bt_ebfc_batch(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t count, uint64_t *sup,
+                        uint64_t *counts);
+
+/* ---- serving --------------------------------------------------------- */
+/*
+ * No reference counterpart (the reference runs one algorithm on one graph per
+ * process).  A server runs count / support / decompose requests on graphs of
+ * different sizes as they arrive.  It has `slots` worker threads, each with
+ * its own context and stream, so their uploads, counting kernels and copies
+ * overlap on the GPU (one peeling kernel runs at a time).  A request is
+ * admitted when a slot is free and its device footprint (bt_job_bytes) fits
+ * in what the HBM budget has left; requests are taken in arrival order, and
+ * one that does not fit yet may be passed by up to 64 later admissions.
+ * Continuous batching: a slot that takes a request also takes every queued
+ * request of the same kind (bfc/ebfc, msp, exact msp) that fits, up to 2^26
+ * edges, and runs them as one arena (bt_msp_batch layout).  Each request's
+ * result is the same alone and in a batch.
+ */
+typedef struct bt_server bt_server;
+
+typedef enum { BT_OP_BFC = 0, BT_OP_EBFC = 1, BT_OP_MSP = 2, BT_OP_MSP_EXACT = 3 } bt_op;
+
+typedef struct {
+    bt_status status;
+    uint64_t count;        /* butterflies (bfc, ebfc) */
+    uint64_t support_max;  /* largest support (ebfc; bfc when batched) */
+    uint32_t levels;       /* msp level count */
+    uint32_t batch_size;   /* requests that shared this request's arena */
+    double queue_ms;       /* submit -> admitted */
+    double run_ms;         /* admitted -> done */
+    double total_ms;       /* submit -> done */
+} bt_request_info;
+
+/* hbm_budget: device bytes the server may hold at once (0 = 90% of the free
+ * memory at creation).  slots: 1..64. */
+bt_status bt_server_create(int device, uint32_t slots, uint64_t hbm_budget, bt_server **out);
+
+/* Queue a request.  op: a bt_op.  out: host buffer for the per-edge result --
+ * m uint32 bitruss numbers (BT_OP_MSP, BT_OP_MSP_EXACT), m uint64 supports
+ * (BT_OP_EBFC) -- or NULL; the graph and `out` must stay valid until the
+ * request is waited for.  *ticket identifies the request. */
+bt_status bt_server_submit(bt_server *s, const bt_graph *g, int op, void *out, uint64_t *ticket);
+
+/* Wait for a request (timeout_ms < 0: no limit).  Returns the request's own
+ * status, or BT_ERR_TIMEOUT if it is not done within the limit (the ticket
+ * stays valid).  A finished ticket is consumed. */
+bt_status bt_server_wait(bt_server *s, uint64_t ticket, double timeout_ms, bt_request_info *info);
+
+/* Latency percentiles (submit -> done, ms) over requests completed since the
+ * server started or the last reset; completed may be NULL. */
+bt_status bt_server_latency(bt_server *s, double *p50_ms, double *p99_ms, uint64_t *completed, int reset);
+
+/* [0] budget, [1] bytes reserved by running jobs, [2] running jobs,
+ * [3] queued requests, [4] batches of more than one request, [5] requests in them. */
+bt_status bt_server_stats(bt_server *s, uint64_t *out, int n);
+
+/* Finish the queued requests, stop the workers, free the contexts. */
+void bt_server_free(bt_server *s);
+
+/* Device bytes a job of `count` graphs (one arena) and this op allocates at
+ * its peak on this context's device: the admission estimate of the server. */
+bt_status bt_job_bytes(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t count, int op, uint64_t *bytes);
 
 /* ---- allocation-free variant ------------------------------------------ */
 
