@@ -77,11 +77,7 @@ L2_FLUSH_BYTES = 512 << 20
 METRIC = "msp bitruss edges/s"
 
 
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+from gpu_bitruss_gb300.replicas import batch_shard, dist_env, max_over_ranks  # noqa: E402
 
 
 def load_peaks():
@@ -262,12 +258,7 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     stats = ctx.stats()
-    t_max = total_ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(total_ms, device=f"cuda:{local}")
     value = world * m * args.steps / (t_max / 1000.0)
 
     # e2e through the public API: H2D upload + msp + D2H of the results
@@ -331,12 +322,14 @@ def run_ours(args):
     return 0
 
 
-def batch_graphs(workload: str):
+def batch_graphs(workload: str, rank: int = 0):
+    """Rank `rank`'s graphs of the batch: batch<N> gives every rank its own
+    run of N graphs (weak scaling across ranks)."""
     from gpu_bitruss_gb300 import gen
     import gpu_bitruss_gb300 as bt
     count = int(workload[len("batch"):])
     sizes = gen.batch_sizes()
-    lists = [gen.batch_graph(i, sizes=sizes) for i in range(count)]
+    lists = [gen.batch_graph(i, sizes=sizes) for i in batch_shard(count, rank, total=len(sizes[0]))]
     graphs = [bt.Graph.from_edges(u, v) for u, v in lists]
     return graphs, lists
 
@@ -351,7 +344,7 @@ def run_batch(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     t_gen = time.perf_counter()
-    graphs, lists = batch_graphs(args.workload)
+    graphs, lists = batch_graphs(args.workload, rank)
     t_gen = time.perf_counter() - t_gen
     count = len(graphs)
     edges = int(sum(g.m for g in graphs))
@@ -396,12 +389,7 @@ def run_batch(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     stats = ctx.stats()
-    t_max = total_ms
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(total_ms, device=f"cuda:{local}")
     value = world * count * args.steps / (t_max / 1000.0)
 
     # e2e: host graphs -> bt_msp_batch -> host results

@@ -285,7 +285,7 @@ struct MspHit {
     const Round &rd;
     uint32_t uv, exact;
     bool piv_is_v;
-    unsigned long long decs = 0;
+    unsigned long long decs = 0, hits = 0;
     struct State {
         uint32_t kslot, e_my, e_ay, ah, en_my, en_ay;
     };
@@ -299,6 +299,7 @@ struct MspHit {
     }
     __device__ __forceinline__ void apply(const State &s) {
         const uint32_t r = rd.r;
+        hits++;  // a butterfly visited (the reference's intersection hit)
         if (is_done(s.en_ay, r) || is_done(s.en_my, r)) return;
         const uint32_t e_pm = w.mid_eid[s.kslot];
         const bool c_pm = w.pm_curr[s.kslot], c_my = s.en_my == r, c_ay = s.en_ay == r;
@@ -393,6 +394,7 @@ __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uin
                 }
             });
         wk.decs += hit.decs;
+        wk.hits += hit.hits;
         bt::prof_mark(w, bt::PF_FLUSH);
         if (a.trace && threadIdx.x == 0 && r < a.trace_cap) {
             atomicMax(&a.trace[r].max_task_ns, bt::global_ns() - task_t0);

@@ -15,7 +15,7 @@
 //
 // Continuous batching: when a slot takes a request, every queued request of
 // the same kind (supports/counts, msp, exact msp) that also fits joins it, up
-// to kBatchEdges edges.  Together they form one arena (bt_graph_pack layout),
+// to kBatchEdges edges; requests above kSoloEdges edges run alone.  Together they form one arena (bt_graph_pack layout),
 // uploaded once and run by one launch sequence.  A request's result is the
 // same alone and in a batch: butterflies never span two graphs of an arena.
 //
@@ -38,6 +38,7 @@
 namespace {
 
 constexpr uint64_t kBatchEdges = 1ull << 26;  // edges per batched arena, at most
+constexpr uint64_t kSoloEdges = 1ull << 22;   // requests above this size run alone
 constexpr uint32_t kMaxBatch = 1024;          // requests per batch, at most
 constexpr uint32_t kMaxSkips = 64;            // admissions that may pass a waiting request
 
@@ -163,12 +164,15 @@ struct bt_server {
             // requests passed over on the way
             for (size_t k = 0; k < qi; k++) queue[k]->skipped++;
             queue.erase(queue.begin() + (long)qi);
-            // continuous batching: later requests of the same kind that fit
+            // continuous batching: later requests of the same kind that fit.
+            // A large request runs alone and small ones never wait behind it:
+            // an arena's peel lasts about as long as its largest graph's.
             const int kind = kind_of(r->op);
             uint64_t edges = r->g->m;
+            if (edges > kSoloEdges) return job;
             for (size_t k = qi; k < queue.size() && job.size() < kMaxBatch;) {
                 ReqPtr q = queue[k];
-                if (kind_of(q->op) != kind || edges + q->g->m > kBatchEdges) {
+                if (kind_of(q->op) != kind || q->g->m > kSoloEdges || edges + q->g->m > kBatchEdges) {
                     k++;
                     continue;
                 }

@@ -220,7 +220,8 @@ bt_status bt_ebfc_batch(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t cou
  * one that does not fit yet may be passed by up to 64 later admissions.
  * Continuous batching: a slot that takes a request also takes every queued
  * request of the same kind (bfc/ebfc, msp, exact msp) that fits, up to 2^26
- * edges, and runs them as one arena (bt_msp_batch layout).  Each request's
+ * edges, and runs them as one arena (bt_msp_batch layout); a request of more
+ * than 2^22 edges runs alone.  Each request's
  * result is the same alone and in a batch.
  */
 typedef struct bt_server bt_server;

@@ -87,8 +87,11 @@ def test_admission_budget(engine, gpu_ctx):
     gd = load_golden("cl20k")
     g = engine.Graph.from_edges(gd["u"], gd["v"])
     need = gpu_ctx.job_bytes([g], "msp")
-    # room for one such job at a time: every request still completes, in turn
-    srv = engine.Server(0, 4, int(need * 1.5))
+    need2 = gpu_ctx.job_bytes([g, g], "msp")
+    assert need2 > need
+    # room for one such job at a time (not for a batch of two): every request
+    # still completes, in turn
+    srv = engine.Server(0, 4, (need + need2) // 2)
     try:
         ts = [srv.submit(g, "msp") for _ in range(6)]
         for t, out in ts:
