@@ -337,7 +337,6 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
     const bool staged = w.cached_size != 0;
     // the anchor row walked in reverse: the live row (staged in this epoch)
     const uint32_t ab = r.off[anc], ad = r.deg[anc];
-    uint32_t par = 0;
     for (uint32_t c0 = s_lo; c0 <= s_hi; c0 += kSliceMids) {
         const uint32_t cl = min(kSliceMids, s_hi + 1 - c0);
         uint32_t cnt = 0;

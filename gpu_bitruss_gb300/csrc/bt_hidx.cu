@@ -20,6 +20,23 @@
 // of 2^36 values needs three passes.  Butterflies are walked as in the
 // peeling kernel (anchor row staged in a shared-memory hash, pivot rows
 // flattened over the block).
+//
+// Active edges: a round only recomputes the edges that can change.  Values
+// only fall, and h_k(e) = min(h_{k-1}(e), hindex(butterfly values of round
+// k-1)), where a butterfly's value is the minimum of its three other edges.
+// An edge keeps h = h_{k-1}(e) as long as at least h butterflies have a
+// value >= h, so it can only change if some butterfly edge f fell, in round
+// k-1, from a value >= h to one below h.  A butterfly of uv = (u, v) has edges
+// ux, wv and wx with x a neighbour of u and w a neighbour of v, so f has an
+// end in N[u] or N[v].  After each round every vertex z holds the lowest new
+// value (lo) and the highest old value (hi) of the changed edges with an end
+// in N[z]; edge (u, v) with value h is recomputed iff lo < h <= hi at u or at
+// v.  The test never skips an edge that could change, so values, and the
+// number of rounds, are those of the full synchronous iteration.
+#include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
 #include <cstdlib>
 
 #include "bt_device.cuh"
@@ -36,10 +53,11 @@ struct HidxArgs {
     const uint2 *ends;
     const uint32_t *two_hop;   // per vertex: row probe total
     const uint32_t *rowpre;    // per slot: prefix of the row's neighbour degrees
-    const unsigned long long *prev;
-    unsigned long long *curr;
-    uint64_t m;
-    unsigned long long *next_edge;  // work counter
+    const unsigned long long *prev;  // values of the last round, by edge id
+    unsigned long long *curr;        // this round's value of active edge k, by list index
+    const uint32_t *active;          // edge ids recomputed this round (ascending)
+    uint64_t m;                      // active edges
+    unsigned long long *next_edge;   // work counter
     unsigned *changed;
 };
 
@@ -136,10 +154,11 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
         const unsigned long long e0 = sm.e0;
         if (e0 >= a.m) break;
         const unsigned long long e1 = e0 + kEdgeChunk < a.m ? e0 + kEdgeChunk : a.m;
-        for (unsigned long long e = e0; e < e1; e++) {
+        for (unsigned long long ei = e0; ei < e1; ei++) {
+            const uint32_t e = a.active[ei];
             const unsigned long long H = prev[e];
             if (H == 0) {  // cpu_bitruss.cpp:155
-                if (threadIdx.x == 0) a.curr[e] = 0;
+                if (threadIdx.x == 0) a.curr[ei] = 0;
                 continue;
             }
             const uint2 uv = a.ends[e];
@@ -202,7 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
                 h = sm.result;
             }
             if (threadIdx.x == 0) {
-                a.curr[e] = h;
+                a.curr[ei] = h;
                 if (h != H) any_change = true;
             }
             __syncthreads();
@@ -213,6 +232,70 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
 
 __global__ void k_row_prefix(bt::Rows r, uint32_t n, uint32_t *rowpre, uint32_t *total) {
     bt::row_prefix(r, n, rowpre, total);
+}
+
+// Apply a round: every active edge whose value changed takes the new value;
+// its endpoints record the lowest new and the highest old value of their
+// changed edges and are listed once (stamp r).
+__global__ void k_hidx_apply(uint64_t len, const uint32_t *active, const unsigned long long *nval,
+                             unsigned long long *val, const uint2 *ends, uint32_t r, uint32_t *mark,
+                             uint32_t *marked, uint32_t *marked_len, unsigned long long *vlo,
+                             unsigned long long *vhi) {
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < len;
+         k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = active[k];
+        const unsigned long long b = nval[k], a = val[e];
+        if (b == a) continue;
+        val[e] = b;
+        const uint2 uv = ends[e];
+        atomicMin(&vlo[uv.x], b);
+        atomicMax(&vhi[uv.x], a);
+        atomicMin(&vlo[uv.y], b);
+        atomicMax(&vhi[uv.y], a);
+        if (atomicExch(&mark[uv.x], r) != r) marked[atomicAdd(marked_len, 1u)] = uv.x;
+        if (atomicExch(&mark[uv.y], r) != r) marked[atomicAdd(marked_len, 1u)] = uv.y;
+    }
+}
+
+// Spread each listed vertex's (lo, hi) to itself and its neighbours (one
+// warp per listed vertex).
+__global__ void k_hidx_near(const uint32_t *marked, const uint32_t *marked_len, bt::Rows rows,
+                            const unsigned long long *vlo, const unsigned long long *vhi,
+                            unsigned long long *nlo, unsigned long long *nhi) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t len = *marked_len;
+    for (uint32_t i = warp; i < len; i += nw) {
+        const uint32_t z = marked[i];
+        const unsigned long long lo = vlo[z], hi = vhi[z];
+        const uint32_t b = rows.off[z], d = rows.deg[z];
+        if (lane == 0) {
+            atomicMin(&nlo[z], lo);
+            atomicMax(&nhi[z], hi);
+        }
+        for (uint32_t j = lane; j < d; j += 32) {
+            const uint32_t y = rows.nbr[b + j];
+            atomicMin(&nlo[y], lo);
+            atomicMax(&nhi[y], hi);
+        }
+    }
+}
+
+// flag of the edges the next round recomputes: value h > 0 with lo < h <= hi
+// at one of its ends
+__global__ void k_hidx_flags(uint64_t m, const unsigned long long *val, const uint2 *ends,
+                             const unsigned long long *nlo, const unsigned long long *nhi, uint8_t *flag) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long h = val[e];
+        bool f = false;
+        if (h > 0) {
+            const uint2 uv = ends[e];
+            f = (nlo[uv.x] < h && h <= nhi[uv.x]) || (nlo[uv.y] < h && h <= nhi[uv.y]);
+        }
+        flag[e] = f ? 1 : 0;
+    }
 }
 
 __global__ void k_hidx_result(uint64_t m, const unsigned long long *v, uint32_t *out, unsigned *overflow) {
@@ -231,23 +314,39 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     DevGraph &g = ctx->g;
     cudaStream_t st = ctx->stream;
     const uint64_t m = g.m, n = g.n;
+    const uint64_t mm = m ? m : 1, nn = n ? n : 1;
     cudaEvent_t e0 = ctx->ev[2], e1 = ctx->ev[3];
     cudaEventRecord(e0, st);
-    unsigned long long *buf_a = nullptr, *buf_b = nullptr, *ctr = nullptr;
-    uint32_t *two_hop = nullptr, *rowpre = nullptr;
+    unsigned long long *val = nullptr, *nval = nullptr, *ctr = nullptr;
+    uint32_t *two_hop = nullptr, *rowpre = nullptr, *active = nullptr, *mark = nullptr;
+    uint32_t *marked = nullptr;
+    unsigned long long *vlo = nullptr, *vhi = nullptr, *nlo = nullptr, *nhi = nullptr;
+    uint8_t *flag = nullptr;
+    void *temp = nullptr;
     auto release = [&]() {
-        ctx_free(ctx, buf_a);
-        ctx_free(ctx, buf_b);
+        ctx_free(ctx, val);
+        ctx_free(ctx, nval);
         ctx_free(ctx, ctr);
         ctx_free(ctx, two_hop);
         ctx_free(ctx, rowpre);
+        ctx_free(ctx, active);
+        ctx_free(ctx, mark);
+        ctx_free(ctx, vlo);
+        ctx_free(ctx, vhi);
+        ctx_free(ctx, nlo);
+        ctx_free(ctx, nhi);
+        ctx_free(ctx, marked);
+        ctx_free(ctx, flag);
+        ctx_free(ctx, temp);
     };
     bt_status rc;
-    if ((rc = ctx_alloc_t(ctx, &buf_a, m ? m : 1)) != BT_OK ||
-        (rc = ctx_alloc_t(ctx, &buf_b, m ? m : 1)) != BT_OK ||
-        (rc = ctx_alloc_t(ctx, &ctr, 4)) != BT_OK ||
-        (rc = ctx_alloc_t(ctx, &two_hop, n ? n : 1)) != BT_OK ||
-        (rc = ctx_alloc_t(ctx, &rowpre, m ? 2 * m : 1)) != BT_OK) {
+    if ((rc = ctx_alloc_t(ctx, &val, mm)) != BT_OK || (rc = ctx_alloc_t(ctx, &nval, mm)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &ctr, 8)) != BT_OK || (rc = ctx_alloc_t(ctx, &two_hop, nn)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &rowpre, 2 * mm)) != BT_OK || (rc = ctx_alloc_t(ctx, &active, mm)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &mark, nn)) != BT_OK || (rc = ctx_alloc_t(ctx, &vlo, nn)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &vhi, nn)) != BT_OK || (rc = ctx_alloc_t(ctx, &nlo, nn)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &nhi, nn)) != BT_OK ||
+        (rc = ctx_alloc_t(ctx, &marked, nn)) != BT_OK || (rc = ctx_alloc_t(ctx, &flag, mm)) != BT_OK) {
         release();
         return rc;
     }
@@ -256,13 +355,27 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
         cudaError_t _e = (x);                                                 \
         if (_e != cudaSuccess) { release(); return bt_cuda_fail(_e, #x, __FILE__, __LINE__); } \
     } while (0)
-    C(cudaMemcpyAsync(buf_a, ctx->sup, 8 * m, cudaMemcpyDeviceToDevice, st));
+    // ctr (uint64 words): [0] work counter, [1] changed, [2] overflow, [3] marked
+    // count, [4] active count
+    uint32_t *marked_len = (uint32_t *)(ctr + 3);
+    unsigned long long *active_len = ctr + 4;
+    C(cudaMemcpyAsync(val, ctx->sup, 8 * m, cudaMemcpyDeviceToDevice, st));
+    C(cudaMemsetAsync(mark, 0, 4 * nn, st));
     bt::Rows rows{g.off, g.deg0, g.nbr0, g.eid0, g.hub_base, g.hub_mask, g.hub_pool};
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
+    const unsigned egrid = (unsigned)std::min<uint64_t>((mm + blk - 1) / blk, cap);
     if (n) {
         k_row_prefix<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(
             rows, g.n, rowpre, two_hop);
         C(cudaGetLastError());
+    }
+    // compaction of flagged edge ids (ascending), temp sized once
+    thrust::counting_iterator<uint32_t> ids(0);
+    size_t tb = 0;
+    C(cub::DeviceSelect::Flagged(nullptr, tb, ids, flag, active, active_len, (int64_t)mm, st));
+    if ((rc = ctx_alloc(ctx, &temp, tb)) != BT_OK) {
+        release();
+        return rc;
     }
     const size_t smem = sizeof(HSmem);
     C(cudaFuncSetAttribute(k_hidx_round, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -270,29 +383,48 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     C(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hidx_round, kThreads, smem));
     if (per_sm < 1) per_sm = 1;
     const unsigned nblocks = (unsigned)(ctx->sm_count * per_sm);
+    // round 1 recomputes every edge
+    uint64_t len = m;
+    if (m) {
+        C(cudaMemsetAsync(flag, 1, m, st));
+        C(cub::DeviceSelect::Flagged(temp, tb, ids, flag, active, active_len, (int64_t)m, st));
+    }
     uint32_t r = 0;
-    unsigned long long *prev = buf_a, *curr = buf_b;
+    uint64_t recomputed = 0;
     for (;;) {
         r++;
+        recomputed += len;
         C(cudaMemsetAsync(ctr, 0, 32, st));
-        HidxArgs a{rows, g.ends, two_hop, rowpre, prev, curr, m, ctr, (unsigned *)(ctr + 1)};
-        if (m) {
+        if (len) {
+            HidxArgs a{rows, g.ends, two_hop, rowpre, val, nval, active, len, ctr, (unsigned *)(ctr + 1)};
             k_hidx_round<<<nblocks, kThreads, smem, st>>>(a);
             C(cudaGetLastError());
         }
         unsigned changed = 0;
         C(cudaMemcpyAsync(&changed, ctr + 1, 4, cudaMemcpyDeviceToHost, st));
         C(cudaStreamSynchronize(st));
-        unsigned long long *t = prev;
-        prev = curr;
-        curr = t;
         if (!changed) break;
+        // apply, then the next round's active edges
+        C(cudaMemsetAsync(vlo, 0xff, 8 * nn, st));
+        C(cudaMemsetAsync(vhi, 0, 8 * nn, st));
+        C(cudaMemsetAsync(nlo, 0xff, 8 * nn, st));
+        C(cudaMemsetAsync(nhi, 0, 8 * nn, st));
+        k_hidx_apply<<<(unsigned)std::min<uint64_t>((len + blk - 1) / blk, cap), blk, 0, st>>>(
+            len, active, nval, val, g.ends, r, mark, marked, marked_len, vlo, vhi);
+        C(cudaGetLastError());
+        k_hidx_near<<<cap, blk, 0, st>>>(marked, marked_len, rows, vlo, vhi, nlo, nhi);
+        C(cudaGetLastError());
+        k_hidx_flags<<<egrid, blk, 0, st>>>(m, val, g.ends, nlo, nhi, flag);
+        C(cudaGetLastError());
+        C(cub::DeviceSelect::Flagged(temp, tb, ids, flag, active, active_len, (int64_t)m, st));
+        unsigned long long nl = 0;
+        C(cudaMemcpyAsync(&nl, active_len, 8, cudaMemcpyDeviceToHost, st));
+        C(cudaStreamSynchronize(st));
+        len = nl;
     }
     unsigned overflow = 0;
-    C(cudaMemsetAsync(ctr + 2, 0, 4, st));
     if (m) {
-        k_hidx_result<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
-            m, prev, ctx->result, (unsigned *)(ctr + 2));
+        k_hidx_result<<<egrid, blk, 0, st>>>(m, val, ctx->result, (unsigned *)(ctr + 2));
         C(cudaGetLastError());
     }
     C(cudaMemcpyAsync(&overflow, ctr + 2, 4, cudaMemcpyDeviceToHost, st));
@@ -305,6 +437,7 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     release();
     if (overflow) return bt_fail(BT_ERR_OVERFLOW, "hidx: a bitruss number exceeds uint32");
     ctx->stats[4] = r;
+    ctx->work[9] = recomputed;  // edge recomputations over all rounds
     ctx->last_result = 2;
     if (rounds) *rounds = r;
     return BT_OK;

@@ -128,3 +128,18 @@ def test_power_law_vs_oracle(engine, gpu_ctx, oracle_mod, name):
     b, lv = gpu_ctx.msp()
     np.testing.assert_array_equal(b.astype(np.uint64), ref)
     assert lv == levels
+
+
+@pytest.mark.parametrize("name", ["aw", "er_config1", "er_small2", "er_small3", "cl5k", "cl20k"])
+def test_hidx_rounds_match_the_oracle(engine, gpu_ctx, oracle_mod, name):
+    """Rounds recompute only edges next to a change, yet take exactly as many
+    rounds as the full synchronous iteration (the reference's count)."""
+    gd = load_golden(name)
+    g = engine.Graph.from_edges(gd["u"], gd["v"])
+    gpu_ctx.upload(g)
+    h, rounds = gpu_ctx.hidx()
+    np.testing.assert_array_equal(h.astype(np.uint64), gd["hidx"])
+    want, want_rounds = oracle_mod.hidx(oracle_mod.build_csr(gd["u"], gd["v"]), 1)
+    assert rounds == want_rounds
+    recomputed = gpu_ctx.stats()[17]
+    assert g.m <= recomputed <= rounds * g.m
