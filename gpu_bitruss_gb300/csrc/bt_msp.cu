@@ -104,7 +104,8 @@ struct MspArgs {
     uint32_t *deg, *nbr, *eid;      // live rows (compacted in place)
     uint32_t *two_hop;              // per vertex: sum of live neighbour degrees (row probe total)
     uint32_t *rowpre;               // per slot: prefix of the row's neighbour degrees
-    unsigned long long *sup;        // working supports
+    unsigned long long *sup;        // working supports (64-bit)
+    uint32_t *sup32;                // working supports when every support fits 32 bits (else null)
     uint32_t *enter;                // sub-round index at which the edge joined a frontier
     uint32_t *result;               // bitruss number per edge
     uint32_t *list[3];              // frontier lists by sub-round index mod 3
@@ -170,8 +171,15 @@ struct Round {
 // clamp at L (update_edge_support, bitruss_msp.cu:110-123) then only matters
 // for the value it is processed with, which is L.  A decrement crossing hi
 // appends e to the near bucket.
+__device__ __forceinline__ unsigned long long sup_of(const MspArgs &a, uint32_t e) {
+    return a.sup32 ? (unsigned long long)a.sup32[e] : a.sup[e];
+}
+
 __device__ __forceinline__ void dec_edge(const MspArgs &a, const Round &rd, uint32_t e, uint32_t k) {
-    const unsigned long long old = atomicAdd(a.sup + e, (unsigned long long)(-(long long)k));
+    // supports never fall below 0: a decrement reaches an edge only while it is
+    // above the level, and each butterfly decrements an edge at most once
+    const unsigned long long old = a.sup32 ? (unsigned long long)atomicSub(a.sup32 + e, k)
+                                           : atomicAdd(a.sup + e, (unsigned long long)(-(long long)k));
     const unsigned long long nw = old - k;
     if (old > rd.L && nw <= rd.L) {
         rd.next[atomicAdd(rd.next_len, 1u)] = e;
@@ -414,7 +422,7 @@ __device__ void list_min(const MspArgs &a, const uint32_t *list, uint32_t len, u
     for (uint32_t i = gtid; i < len; i += gsz) {
         const uint32_t e = list[i];
         if (a.enter[e] == 0) {
-            const unsigned long long s = a.sup[e];
+            const unsigned long long s = sup_of(a, e);
             v = s < v ? s : v;
         }
     }
@@ -501,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
                 for (uint32_t i = gtid; i < s->far_len; i += gsz) {
                     const uint32_t e = a.far_a[i];
                     if (a.enter[e] != 0) continue;
-                    if (a.sup[e] < hi) a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
+                    if (sup_of(a, e) < hi) a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
                     else a.far_b[atomicAdd(&s->far2_len, 1u)] = e;
                 }
                 if (!barrier(a, sm)) return;
@@ -531,7 +539,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
             for (uint32_t i = gtid; i < near_len; i += gsz) {
                 const uint32_t e = a.near_a[i];
                 if (a.enter[e] != 0) continue;
-                if (a.sup[e] == L) {
+                if (sup_of(a, e) == L) {
                     a.enter[e] = r;
                     a.result[e] = (uint32_t)L;
                     front[atomicAdd(&s->len[r % 3], 1u)] = e;
@@ -643,11 +651,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
 // ---------------------------------------------------------------------------
 
 __global__ void k_msp_init(uint64_t m, const unsigned long long *sup_in, unsigned long long *sup,
-                           uint32_t *enter, uint32_t *result, uint32_t *far_list, MspState *s) {
+                           uint32_t *sup32, uint32_t *enter, uint32_t *result, uint32_t *far_list, MspState *s) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
          e += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long v = sup_in[e];
-        sup[e] = v;
+        if (sup32) sup32[e] = (uint32_t)v;  // every support fits (checked on the host)
+        else sup[e] = v;
         result[e] = 0;
         if (v == 0) {
             enter[e] = 1;  // processed first (count_es_zero, bitruss_msp.cu:38-50)
@@ -706,7 +715,13 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     A(a.nbr, 8 * mm);
     A(a.eid, 8 * mm);
     A(a.two_hop, 4 * nn);
-    A(a.sup, 8 * mm);
+    // 32-bit working supports when they all fit: half the footprint and
+    // 4-byte atomics for the decrements
+    // (BT_MSP_WIDE=1 keeps 64-bit supports: the path graphs with a support
+    // above 2^32 take, testable on small graphs)
+    const char *wide = getenv("BT_MSP_WIDE");
+    if (ctx->last_sup_max <= 0xffffffffull && !(wide && *wide == '1')) A(a.sup32, 4 * mm);
+    else A(a.sup, 8 * mm);
     A(a.enter, 4 * mm);
     A(a.list[0], 4 * mm);
     A(a.list[1], 4 * mm);
@@ -763,7 +778,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (m) {
         k_msp_init<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
-            m, (const unsigned long long *)ctx->sup, a.sup, a.enter, a.result, a.far_a, s);
+            m, (const unsigned long long *)ctx->sup, a.sup, a.sup32, a.enter, a.result, a.far_a, s);
         C(cudaGetLastError());
     }
     // edge_num = live edges

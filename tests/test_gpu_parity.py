@@ -143,3 +143,18 @@ def test_hidx_rounds_match_the_oracle(engine, gpu_ctx, oracle_mod, name):
     assert rounds == want_rounds
     recomputed = gpu_ctx.stats()[17]
     assert g.m <= recomputed <= rounds * g.m
+
+
+@pytest.mark.parametrize("name", ["aw", "er_config1", "er_small3", "cl5k", "cl20k"])
+def test_msp_with_64bit_working_supports(engine, gpu_ctx, name, monkeypatch):
+    """Graphs whose supports all fit 32 bits peel with 32-bit working supports;
+    the 64-bit path (supports above 2^32) gives the same results."""
+    gd = load_golden(name)
+    g = engine.Graph.from_edges(gd["u"], gd["v"])
+    gpu_ctx.upload(g)
+    monkeypatch.setenv("BT_MSP_WIDE", "1")
+    b, levels = gpu_ctx.msp()
+    np.testing.assert_array_equal(b.astype(np.uint64), gd["msp"])
+    assert levels == int(gd["levels"])
+    x, _ = gpu_ctx.msp(exact=True)
+    np.testing.assert_array_equal(x.astype(np.uint64), gd["hidx"])
