@@ -238,7 +238,7 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     total_ms, peel_ms, work = 0.0, [], None
-    launches = 0
+    launches0 = bt.kernel_launches()
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1)
@@ -253,8 +253,8 @@ def run_ours(args):
         peel_ms.append(ctx.phase_ms("peel"))
         st = ctx.stats()
         work = st[8:17]
-        launches += 5  # k_count, k_msp_init, k_two_hop, k_msp, k_msp_result
     torch.cuda.synchronize()
+    launches = bt.kernel_launches() - launches0  # k_count, k_msp_init, k_two_hop, k_msp per step
     barrier()
     clk = clocks.stop()
     stats = ctx.stats()
@@ -374,6 +374,7 @@ def run_batch(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     total_ms, peel_ms = 0.0, []
+    launches0 = bt.kernel_launches()
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1)
@@ -387,6 +388,7 @@ def run_batch(args):
         total_ms += e0.elapsed_time(e1)
         peel_ms.append(ctx.phase_ms("peel"))
     torch.cuda.synchronize()
+    launches = bt.kernel_launches() - launches0
     clk = clocks.stop()
     stats = ctx.stats()
     t_max = max_over_ranks(total_ms, device=f"cuda:{local}")
@@ -431,7 +433,7 @@ def run_batch(args):
         "per_graph_loop": {"device_graphs_per_s": count / (loop_dev_ms / 1000.0),
                            "e2e_graphs_per_s": count / loop_wall,
                            "results_equal_batched": mismatch == 0},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": launches,
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu:
@@ -493,6 +495,7 @@ def run_serve(args):
     ctx.close()
 
     per_rate = []
+    launches0 = bt.kernel_launches()
     for rate in [float(r) for r in args.rates.split(",")]:
         srv = bt.Server(0, args.slots, 160 << 30)
         gaps = rng.exponential(1.0 / rate, size=nreq)
@@ -524,6 +527,7 @@ def run_serve(args):
         per_rate.append({"rate_req_s": rate, "graphs_per_s": nreq / (end - start),
                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                          "batched_requests": int(batched), "batches": int(st["batches"])})
+    launches = bt.kernel_launches() - launches0
     iso = np.array(iso)
     best = max(per_rate, key=lambda r: r["graphs_per_s"])
     line = {
@@ -541,7 +545,7 @@ def run_serve(args):
                 "h2d_bytes_per_step": int(sum(4 * (g.n + 1) + 4 * g.n + 16 * g.m for g, _ in reqs)),
                 "d2h_bytes_per_step": int(sum((4 if op == "msp" else 8 if op == "ebfc" else 0) * g.m
                                               for g, op in reqs))},
-        "gpu_launches": None,
+        "gpu_launches": launches,
     }
     print(json.dumps(line), flush=True)
     return 0

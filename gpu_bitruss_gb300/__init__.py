@@ -53,6 +53,7 @@ SYMBOLS = [
     "bt_graph_pack", "bt_ctx_set_arena_edges", "bt_msp_batch", "bt_ebfc_batch",
     "bt_ctx_memory_peak", "bt_server_create", "bt_server_submit", "bt_server_wait",
     "bt_server_latency", "bt_server_stats", "bt_server_free", "bt_job_bytes",
+    "bt_kernel_launches",
 ]
 
 OPS = {"bfc": 0, "ebfc": 1, "msp": 2, "msp_exact": 3}
@@ -139,6 +140,7 @@ def load():
         "bt_server_stats": ([P, C.POINTER(u64), i32], i32),
         "bt_server_free": ([P], None),
         "bt_job_bytes": ([P, P, u32, i32, C.POINTER(u64)], i32),
+        "bt_kernel_launches": ([], u64),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -477,6 +479,11 @@ def bfc_noalloc(device: int, d_offsets: int, d_neighbors: int, n: int, m: int,
     without any device allocation by the library; enqueued on `stream`."""
     _check(load().bt_bfc_noalloc(device, C.c_void_p(d_offsets), C.c_void_p(d_neighbors), n, m,
                                  C.c_void_p(d_count), C.c_void_p(stream or 0)), "bt_bfc_noalloc")
+
+
+def kernel_launches() -> int:
+    """The library's own kernel launches in this process so far."""
+    return int(load().bt_kernel_launches())
 
 
 def bitruss_msp_exact(g: Graph) -> np.ndarray:

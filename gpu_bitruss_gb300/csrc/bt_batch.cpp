@@ -167,6 +167,7 @@ extern "C" bt_status bt_ctx_set_arena_edges(bt_ctx *ctx, uint64_t edges) {
 
 extern "C" bt_status bt_msp_batch(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t count, int exact,
                                   uint32_t *bitruss, uint32_t *levels) {
+    NvtxRange range("bt_msp_batch");
     BT_TRY(enter_ctx(ctx));
     BT_TRY(check_graphs(graphs, count));
     const double t0 = now_ms();
@@ -220,6 +221,7 @@ extern "C" bt_status bt_msp_batch(bt_ctx *ctx, const bt_graph *const *graphs, ui
 
 extern "C" bt_status bt_ebfc_batch(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t count, uint64_t *sup,
                                    uint64_t *counts) {
+    NvtxRange range("bt_ebfc_batch");
     BT_TRY(enter_ctx(ctx));
     BT_TRY(check_graphs(graphs, count));
     const double t0 = now_ms();

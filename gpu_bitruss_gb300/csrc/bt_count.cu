@@ -179,6 +179,7 @@ bt_status dev_ebfc(bt_ctx *ctx, bool per_edge, uint64_t *count) {
     if (g.n) {
         if (per_edge) k_count<true><<<(unsigned)nctas, kCountThreads, 0, st>>>(a);
         else k_count<false><<<(unsigned)nctas, kCountThreads, 0, st>>>(a);
+        bt_note_launches(1);
         BT_CUDA(cudaGetLastError());
     }
     cudaEventRecord(ctx->ev[7], st);

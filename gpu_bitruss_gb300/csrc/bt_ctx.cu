@@ -8,6 +8,7 @@
 #include <cub/device/device_segmented_sort.cuh>
 
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -37,6 +38,10 @@ bt_status bt_cuda_fail(cudaError_t e, const char *what, const char *file, int li
 }
 
 extern "C" const char *bt_last_error(void) { return t_last_error.c_str(); }
+
+static std::atomic<uint64_t> g_kernel_launches{0};
+void bt_note_launches(uint64_t k) { g_kernel_launches.fetch_add(k, std::memory_order_relaxed); }
+extern "C" uint64_t bt_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 extern "C" const char *bt_status_string(bt_status s) {
     switch (s) {
@@ -427,19 +432,19 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
 
     unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (n) {
-        k_rank_keys<<<grid_for(n, blk, cap), blk, 0, st>>>(n, s_deg, keys, vals);
+        k_rank_keys<<<grid_for(n, blk, cap), blk, 0, st>>>(n, s_deg, keys, vals); bt_note_launches(1);
         STEPC(cub::DeviceRadixSort::SortPairs(temp, t1, keys, keys2, vals, order, (int)n, 0, 64, st));
         if (segmented) {
             // group the ranks by graph, priority order kept within a graph (stable sort)
-            k_gather_seg<<<grid_for(n, blk, cap), blk, 0, st>>>(n, order, s_seg, seg_r);
+            k_gather_seg<<<grid_for(n, blk, cap), blk, 0, st>>>(n, order, s_seg, seg_r); bt_note_launches(1);
             size_t t5 = tb;
             STEPC(cub::DeviceRadixSort::SortPairs(temp, t5, seg_r, seg_r2, order, order2, (int)n, 0, seg_bits,
                                                   st));
             std::swap(order, order2);
-            k_seg_base<<<grid_for(n, blk, cap), blk, 0, st>>>(n, seg_r2, g.seg_base);
+            k_seg_base<<<grid_for(n, blk, cap), blk, 0, st>>>(n, seg_r2, g.seg_base); bt_note_launches(1);
             STEPC(cudaGetLastError());
         }
-        k_rank_scatter<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.u_num, order, s_deg, rank, g.deg0, g.is_u);
+        k_rank_scatter<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.u_num, order, s_deg, rank, g.deg0, g.is_u); bt_note_launches(1);
     }
     // off = exclusive scan of deg0 over n+1 entries (deg0[n] read as garbage is
     // avoided by scanning n entries and setting off[n] = 2m)
@@ -451,7 +456,7 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
     }
     if (n) {
         k_rows_relabel<<<grid_for((uint64_t)n * 32, blk, cap), blk, 0, st>>>(n, g.u_num, s_off, s_nbr, s_eid,
-                                                                              rank, g.off, t_nbr, t_eid, g.ends);
+                                                                              rank, g.off, t_nbr, t_eid, g.ends); bt_note_launches(1);
         STEPC(cudaGetLastError());
     }
     if (m) {
@@ -462,7 +467,7 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
     STEP(ctx_alloc_t(ctx, &g.hub_base, n ? n : 1));
     STEP(ctx_alloc_t(ctx, &g.hub_mask, n ? n : 1));
     if (n) {
-        k_hub_sizes<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.deg0, order, g.hub_mask);
+        k_hub_sizes<<<grid_for(n, blk, cap), blk, 0, st>>>(n, g.deg0, order, g.hub_mask); bt_note_launches(1);
         STEPC(cudaGetLastError());
         size_t t4 = 0;
         STEPC(cub::DeviceScan::ExclusiveSum(nullptr, t4, order, g.hub_base, (int)n, st));
@@ -483,7 +488,7 @@ bt_status dev_build_graph(bt_ctx *ctx, const bt_graph *hg) {
     if (g.hub_slots) {
         STEPC(cudaMemsetAsync(g.hub_pool, 0xff, 8 * g.hub_slots, st));
         bt::Rows rows{g.off, g.deg0, g.nbr0, g.eid0, g.hub_base, g.hub_mask, g.hub_pool};
-        k_hub_build<<<(unsigned)ctx->sm_count * 4, 256, 0, st>>>(rows, n, g.hub_pool);
+        k_hub_build<<<(unsigned)ctx->sm_count * 4, 256, 0, st>>>(rows, n, g.hub_pool); bt_note_launches(1);
         STEPC(cudaGetLastError());
     }
     STEPC(cudaStreamSynchronize(st));
@@ -522,6 +527,7 @@ static void time_end(bt_ctx *ctx, int phase) {
 }
 
 extern "C" bt_status bt_graph_upload(bt_ctx *ctx, const bt_graph *g) {
+    NvtxRange range("bt_graph_upload");
     BT_TRY(enter(ctx));
     if (!g) return bt_fail(BT_ERR_INVALID, "null graph");
     time_begin(ctx);
@@ -538,6 +544,7 @@ static bt_status copy_out(bt_ctx *ctx, void *host, const void *dev, uint64_t byt
 }
 
 extern "C" bt_status bt_bfc(bt_ctx *ctx, uint64_t *count) {
+    NvtxRange range("bt_bfc");
     BT_TRY(need_graph(ctx));
     time_begin(ctx);
     uint64_t c = 0;
@@ -548,6 +555,7 @@ extern "C" bt_status bt_bfc(bt_ctx *ctx, uint64_t *count) {
 }
 
 extern "C" bt_status bt_ebfc(bt_ctx *ctx, uint64_t *sup, uint64_t *count, uint64_t *support_max) {
+    NvtxRange range("bt_ebfc");
     BT_TRY(need_graph(ctx));
     time_begin(ctx);
     uint64_t c = 0;
@@ -559,6 +567,7 @@ extern "C" bt_status bt_ebfc(bt_ctx *ctx, uint64_t *sup, uint64_t *count, uint64
 }
 
 extern "C" bt_status bt_msp(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels) {
+    NvtxRange range("bt_msp");
     BT_TRY(need_graph(ctx));
     time_begin(ctx);
     uint32_t lv = 0;
@@ -569,6 +578,7 @@ extern "C" bt_status bt_msp(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels) {
 }
 
 extern "C" bt_status bt_msp_exact(bt_ctx *ctx, uint32_t *bitruss, uint32_t *levels) {
+    NvtxRange range("bt_msp_exact");
     BT_TRY(need_graph(ctx));
     time_begin(ctx);
     uint32_t lv = 0;
@@ -579,6 +589,7 @@ extern "C" bt_status bt_msp_exact(bt_ctx *ctx, uint32_t *bitruss, uint32_t *leve
 }
 
 extern "C" bt_status bt_hidx(bt_ctx *ctx, uint32_t *bitruss, uint32_t *rounds) {
+    NvtxRange range("bt_hidx");
     BT_TRY(need_graph(ctx));
     time_begin(ctx);
     uint32_t r = 0;

@@ -366,7 +366,7 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     const unsigned egrid = (unsigned)std::min<uint64_t>((mm + blk - 1) / blk, cap);
     if (n) {
         k_row_prefix<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(
-            rows, g.n, rowpre, two_hop);
+            rows, g.n, rowpre, two_hop); bt_note_launches(1);
         C(cudaGetLastError());
     }
     // compaction of flagged edge ids (ascending), temp sized once
@@ -397,7 +397,7 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
         C(cudaMemsetAsync(ctr, 0, 32, st));
         if (len) {
             HidxArgs a{rows, g.ends, two_hop, rowpre, val, nval, active, len, ctr, (unsigned *)(ctr + 1)};
-            k_hidx_round<<<nblocks, kThreads, smem, st>>>(a);
+            k_hidx_round<<<nblocks, kThreads, smem, st>>>(a); bt_note_launches(1);
             C(cudaGetLastError());
         }
         unsigned changed = 0;
@@ -410,11 +410,11 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
         C(cudaMemsetAsync(nlo, 0xff, 8 * nn, st));
         C(cudaMemsetAsync(nhi, 0, 8 * nn, st));
         k_hidx_apply<<<(unsigned)std::min<uint64_t>((len + blk - 1) / blk, cap), blk, 0, st>>>(
-            len, active, nval, val, g.ends, r, mark, marked, marked_len, vlo, vhi);
+            len, active, nval, val, g.ends, r, mark, marked, marked_len, vlo, vhi); bt_note_launches(1);
         C(cudaGetLastError());
-        k_hidx_near<<<cap, blk, 0, st>>>(marked, marked_len, rows, vlo, vhi, nlo, nhi);
+        k_hidx_near<<<cap, blk, 0, st>>>(marked, marked_len, rows, vlo, vhi, nlo, nhi); bt_note_launches(1);
         C(cudaGetLastError());
-        k_hidx_flags<<<egrid, blk, 0, st>>>(m, val, g.ends, nlo, nhi, flag);
+        k_hidx_flags<<<egrid, blk, 0, st>>>(m, val, g.ends, nlo, nhi, flag); bt_note_launches(1);
         C(cudaGetLastError());
         C(cub::DeviceSelect::Flagged(temp, tb, ids, flag, active, active_len, (int64_t)m, st));
         unsigned long long nl = 0;
@@ -424,7 +424,7 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     }
     unsigned overflow = 0;
     if (m) {
-        k_hidx_result<<<egrid, blk, 0, st>>>(m, val, ctx->result, (unsigned *)(ctr + 2));
+        k_hidx_result<<<egrid, blk, 0, st>>>(m, val, ctx->result, (unsigned *)(ctr + 2)); bt_note_launches(1);
         C(cudaGetLastError());
     }
     C(cudaMemcpyAsync(&overflow, ctr + 2, 4, cudaMemcpyDeviceToHost, st));

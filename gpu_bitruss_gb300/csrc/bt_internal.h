@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -28,6 +29,19 @@ bt_status bt_cuda_fail(cudaError_t e, const char *what, const char *file, int li
         bt_status _s = (call);                                               \
         if (_s != BT_OK) return _s;                                          \
     } while (0)
+
+// Count of this library's own kernel launches (every launch site adds its
+// launches; read by bt_kernel_launches).
+void bt_note_launches(uint64_t k);
+
+// NVTX range over a scope: each public call shows up as a named range on a
+// profiler's timeline (no cost without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // host graph: the reference's Graph fields (src/graph/graph.h:43-51)

@@ -778,7 +778,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     if (m) {
         k_msp_init<<<(unsigned)std::min<uint64_t>((m + blk - 1) / blk, cap), blk, 0, st>>>(
-            m, (const unsigned long long *)ctx->sup, a.sup, a.sup32, a.enter, a.result, a.far_a, s);
+            m, (const unsigned long long *)ctx->sup, a.sup, a.sup32, a.enter, a.result, a.far_a, s); bt_note_launches(1);
         C(cudaGetLastError());
     }
     // edge_num = live edges
@@ -790,7 +790,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
         C(cudaMemcpyAsync(s, &h0, sizeof(MspState), cudaMemcpyHostToDevice, st));
     }
     if (n) {
-        k_two_hop<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(a);
+        k_two_hop<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(a); bt_note_launches(1);
         C(cudaGetLastError());
     }
     // cooperative persistent launch
@@ -805,6 +805,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     // grid barrier for CTAs that cannot be placed.  Contexts on other streams
     // (serving slots) still overlap their counting, uploads and copies.
     std::unique_lock<std::mutex> coop(g_coop_mutex, std::defer_lock);
+    NvtxRange range("k_msp");
     if (m) {
         coop.lock();
         void *params[] = {&a};
@@ -817,6 +818,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
             return bt_cuda_fail(le, "cudaLaunchCooperativeKernel(k_msp)", __FILE__, __LINE__);
         }
         cudaEventRecord(ctx->ev[5], st);
+        bt_note_launches(1);
     }
     cudaEventRecord(e1, st);
     MspState h{};

@@ -139,7 +139,7 @@ extern "C" bt_status bt_bfc_noalloc(int device, const uint32_t *d_offsets, const
     const uint64_t fit = kScratchWords / (2ull * n);
     if (ctas > fit) ctas = fit;
     if (ctas > n) ctas = n;
-    k_bfc_noalloc<<<(unsigned)ctas, kThreadsNA, 0, st>>>(n, d_offsets, d_neighbors, scratch, counter, d_count);
+    k_bfc_noalloc<<<(unsigned)ctas, kThreadsNA, 0, st>>>(n, d_offsets, d_neighbors, scratch, counter, d_count); bt_note_launches(1);
     BT_CUDA(cudaGetLastError());
     return BT_OK;
 }

@@ -195,6 +195,7 @@ struct bt_server {
 };
 
 void bt_server::run_job(bt_ctx *ctx, std::vector<ReqPtr> &job, uint64_t need) {
+    NvtxRange range("bt_server_job");
     const int kind = kind_of(job[0]->op);
     ctx->budget = need;
     ctx->peak = ctx->used;

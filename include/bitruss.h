@@ -289,6 +289,10 @@ bt_status bt_job_bytes(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t coun
 bt_status bt_bfc_noalloc(int device, const uint32_t *d_offsets, const uint32_t *d_neighbors,
                          uint32_t n, uint64_t m, unsigned long long *d_count, void *stream);
 
+/* Number of the library's own kernel launches in this process so far (CUB
+ * launches inside the library are not counted).  No reference counterpart. */
+uint64_t bt_kernel_launches(void);
+
 /* ---- errors ---------------------------------------------------------- */
 
 const char *bt_status_string(bt_status s);

@@ -158,3 +158,15 @@ def test_msp_with_64bit_working_supports(engine, gpu_ctx, name, monkeypatch):
     assert levels == int(gd["levels"])
     x, _ = gpu_ctx.msp(exact=True)
     np.testing.assert_array_equal(x.astype(np.uint64), gd["hidx"])
+
+
+def test_kernel_launch_count(engine, gpu_ctx):
+    """A bt_msp call on a resident graph launches the library's own kernels
+    k_count, k_msp_init, k_two_hop and the persistent k_msp: four launches,
+    whatever the number of levels and sub-rounds."""
+    gd = load_golden("cl20k")
+    g = engine.Graph.from_edges(gd["u"], gd["v"])
+    gpu_ctx.upload(g)
+    before = engine.kernel_launches()
+    gpu_ctx.msp()
+    assert engine.kernel_launches() - before == 4
