@@ -172,14 +172,14 @@ __device__ inline void walk_stage(const Rows &r, Walk &w, uint32_t anc, uint32_t
         __syncthreads();
         return;
     }
-    const uint32_t d = r.deg[anc];
+    const uint32_t d = r.deg[anc], b = r.off[anc];
     for (uint32_t t = threadIdx.x; t < w.cached_size; t += blockDim.x) w.hkey[t] = kEmpty;
     __syncthreads();
     uint32_t size = 0;
     if (d <= kHashMaxDeg) {
         size = 64;
         while (size < 2 * d) size <<= 1;
-        const uint32_t mask = size - 1, b = r.off[anc];
+        const uint32_t mask = size - 1;
         for (uint32_t j = threadIdx.x; j < d; j += blockDim.x) {
             const uint32_t y = r.nbr[b + j], e = r.eid[b + j];
             uint32_t h = hash_slot(y, mask);
@@ -309,11 +309,12 @@ __device__ inline uint32_t warp_find_slot(const uint32_t *pre, uint32_t d, uint3
 // 32 * kPerThread positions (kPerThread consecutive ones per lane) on its own
 // and hands every hit -- y != piv adjacent to both mid and anc -- to on_hit
 // right away, in two steps so that the memory traffic of a lane's hits
-// overlaps: on_hit.load(state, k, e_my, a) (loads only) for all of them, then
-// on_hit.apply(state) for each.  k =
+// overlaps: on_hit.load(state, k, e_my, a) (loads only) for all of them,
+// on_hit.apply(state) for each, then on_hit.settle(state) for each.  k =
 // slice slot of mid (| kRevHit for a reverse hit), e_my = the edge id
 // (mid, y), a = the anchor's answer for y (walk_lookup's convention: a hash
-// slot when anc is staged, else the edge id).  slice_done(cl, last) runs
+// slot when anc is staged, else the edge id), then on_hit.settle(state) for
+// each (results of atomics that apply issued).  slice_done(cl, last) runs
 // (block-uniform) after each slice's last hit; last marks the final slice.
 template <class PrepSlot, class OnHit, class SliceDone>
 __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w, uint32_t piv,
@@ -348,19 +349,21 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
             const uint32_t p1 = slot + 1 < pd ? pre[slot + 1] : total;
             const uint32_t lo = max(f0, p0), hi = min(f1, p1);
             const uint32_t dk = p1 - p0;
+            // mid's hub index and row start travel with the slot's own loads
+            // (mid < n always): one round trip instead of three
+            const uint32_t hm = r.hub_mask[mid], hb = r.hub_base[mid], mo = r.off[mid];
             bool ok = lo < hi && mid != anc;
             ok = ok && prep_slot(threadIdx.x, e_pm);
             uint32_t mask = 0, base = 0, j0 = 0;
             if (ok) {
-                const uint32_t hm = r.hub_mask[mid];
                 if (hm && ad < dk) {  // reverse: walk anc's row, look up in mid's table
                     mask = hm;
-                    base = r.hub_base[mid];
+                    base = hb;
                     j0 = (uint32_t)((unsigned long long)(lo - p0) * ad / dk);
                     const uint32_t j1 = (uint32_t)((unsigned long long)(hi - p0) * ad / dk);
                     cnt = j1 - j0;
                 } else {
-                    base = r.off[mid];
+                    base = mo;
                     j0 = lo - p0;
                     cnt = hi - lo;
                 }
@@ -458,6 +461,9 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
 #pragma unroll
             for (uint32_t p = 0; p < kPerThread; p++)
                 if (hitmask & (1u << p)) on_hit.apply(hs[p]);
+#pragma unroll
+            for (uint32_t p = 0; p < kPerThread; p++)
+                if (hitmask & (1u << p)) on_hit.settle(hs[p]);
         }
         __syncthreads();
         prof_mark(w, PF_PROBE);

@@ -81,6 +81,7 @@ struct CountHits {
         K++;
         if (v >= H) cge++;
     }
+    __device__ __forceinline__ void settle(const State &) const {}
 };
 
 // a refinement pass: histogram of the values in [lo, hi), count of those >= hi
@@ -104,6 +105,7 @@ struct BinHits {
         if (v >= hi) above++;
         else if (v >= lo) atomicAdd(&hist[(v - lo) / width], 1u);
     }
+    __device__ __forceinline__ void settle(const State &) const {}
 };
 
 struct HSmem {

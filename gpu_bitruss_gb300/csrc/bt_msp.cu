@@ -47,6 +47,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
+#include <type_traits>
 
 #include "bt_device.cuh"
 #include "bt_internal.h"
@@ -171,15 +172,30 @@ struct Round {
 // clamp at L (update_edge_support, bitruss_msp.cu:110-123) then only matters
 // for the value it is processed with, which is L.  A decrement crossing hi
 // appends e to the near bucket.
+// The kernel is compiled twice: N32 = every working support fits 32 bits
+// (4-byte supports and atomics), else 64-bit supports.
+template <bool N32>
+using SupWord = typename std::conditional<N32, uint32_t, unsigned long long>::type;
+
+template <bool N32>
 __device__ __forceinline__ unsigned long long sup_of(const MspArgs &a, uint32_t e) {
-    return a.sup32 ? (unsigned long long)a.sup32[e] : a.sup[e];
+    if constexpr (N32) return a.sup32[e];
+    else return a.sup[e];
 }
 
-__device__ __forceinline__ void dec_edge(const MspArgs &a, const Round &rd, uint32_t e, uint32_t k) {
+// A decrement is split in two so that a thread can have several in flight:
+// dec_issue sends the atomic and returns the old support (nothing waits for
+// it until the value is used), dec_settle acts on the crossings it shows.
+template <bool N32>
+__device__ __forceinline__ SupWord<N32> dec_issue(const MspArgs &a, uint32_t e, uint32_t k) {
     // supports never fall below 0: a decrement reaches an edge only while it is
     // above the level, and each butterfly decrements an edge at most once
-    const unsigned long long old = a.sup32 ? (unsigned long long)atomicSub(a.sup32 + e, k)
-                                           : atomicAdd(a.sup + e, (unsigned long long)(-(long long)k));
+    if constexpr (N32) return atomicSub(a.sup32 + e, k);
+    else return atomicAdd(a.sup + e, (unsigned long long)(-(long long)k));
+}
+
+__device__ __forceinline__ void dec_settle(const MspArgs &a, const Round &rd, uint32_t e, uint32_t k,
+                                           unsigned long long old) {
     const unsigned long long nw = old - k;
     if (old > rd.L && nw <= rd.L) {
         rd.next[atomicAdd(rd.next_len, 1u)] = e;
@@ -287,6 +303,7 @@ __device__ void plan(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t 
 
 // The rule applied to the butterflies of one frontier edge uv (see
 // bt::walk_range for the two-step interface).
+template <bool N32>
 struct MspHit {
     const MspArgs &a;
     bt::Walk &w;
@@ -296,6 +313,10 @@ struct MspHit {
     unsigned long long decs = 0, hits = 0;
     struct State {
         uint32_t kslot, e_my, e_ay, ah, en_my, en_ay;
+        // old supports of the global decrements this hit has in flight, 0 for
+        // none (a decremented edge's old support is at least 1: an edge loses
+        // at most one support per butterfly it is in)
+        SupWord<N32> old_my, old_ay;
     };
     __device__ __forceinline__ void load(State &s, uint32_t kk, uint32_t e_my, uint32_t ah) const {
         s.kslot = kk & ~(uint32_t)bt::kRevHit;
@@ -305,9 +326,13 @@ struct MspHit {
         s.en_my = a.enter[e_my];
         s.en_ay = a.enter[s.e_ay];
     }
-    __device__ __forceinline__ void apply(const State &s) {
+    // The rule for one hit.  Pivot-side and staged anchor-side decrements are
+    // summed in shared memory; the others are issued here and settled by
+    // settle() once every hit of the lane has issued its own.
+    __device__ __forceinline__ void apply(State &s) {
         const uint32_t r = rd.r;
         hits++;  // a butterfly visited (the reference's intersection hit)
+        s.old_my = s.old_ay = 0;
         if (is_done(s.en_ay, r) || is_done(s.en_my, r)) return;
         const uint32_t e_pm = w.mid_eid[s.kslot];
         const bool c_pm = w.pm_curr[s.kslot], c_my = s.en_my == r, c_ay = s.en_ay == r;
@@ -323,14 +348,19 @@ struct MspHit {
         const bool dec_ay = piv_is_v ? d_ux : d_wv;
         decs += (uint32_t)dec_pm + (uint32_t)d_wx + (uint32_t)dec_ay;
         if (dec_pm) atomicAdd(&w.slot_dec[s.kslot], 1u);
-        if (d_wx) dec_edge(a, rd, s.e_my, 1);
+        if (d_wx) s.old_my = dec_issue<N32>(a, s.e_my, 1);
         if (dec_ay) {
             if (w.cached_size) atomicAdd(&w.hdec[s.ah], 1u);
-            else dec_edge(a, rd, s.e_ay, 1);
+            else s.old_ay = dec_issue<N32>(a, s.e_ay, 1);
         }
+    }
+    __device__ __forceinline__ void settle(const State &s) const {
+        if (s.old_my) dec_settle(a, rd, s.e_my, 1, s.old_my);
+        if (s.old_ay) dec_settle(a, rd, s.e_ay, 1, s.old_ay);
     }
 };
 
+template <bool N32>
 __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uint32_t curr_len,
                            const uint32_t *pl_piv, const uint32_t *pl_anc, const uint32_t *pl_grain,
                            const uint32_t *pl_total, const uint32_t *start, uint32_t ntasks, uint32_t *ctr,
@@ -371,7 +401,7 @@ __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uin
         const uint32_t exact = a.exact;
         if (threadIdx.x == 0) wk.mids++;
         bt::prof_mark(w, bt::PF_TASK);
-        MspHit hit{a, w, rd, uv, exact, piv_is_v};
+        MspHit<N32> hit{a, w, rd, uv, exact, piv_is_v};
         bt::walk_range(
             rows, a.rowpre, w, piv, anc, epoch, total, f0, f1,
             [&](uint32_t kk, uint32_t e_pm) {
@@ -383,23 +413,38 @@ __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uin
             [&](uint32_t cl, bool last) {
                 // flush the pivot-side decrements of the slice and, after the
                 // last slice, the anchor-side decrements of the task
+                // (every decrement of a thread is issued before any is settled)
                 __syncthreads();
+                uint32_t c = 0;
+                SupWord<N32> old = 0;
                 if (threadIdx.x < cl) {
-                    const uint32_t c = w.slot_dec[threadIdx.x];
+                    c = w.slot_dec[threadIdx.x];
                     if (c) {
                         w.slot_dec[threadIdx.x] = 0;
-                        dec_edge(a, rd, w.mid_eid[threadIdx.x], c);
+                        old = dec_issue<N32>(a, w.mid_eid[threadIdx.x], c);
                     }
                 }
-                if (last && w.cached_size) {
-                    for (uint32_t h = threadIdx.x; h < w.cached_size; h += kThreads) {
-                        const uint32_t c = w.hdec[h];
-                        if (c) {
+                constexpr uint32_t kPer = bt::kHashSlots / kThreads;
+                uint32_t hc[kPer];
+                SupWord<N32> hold[kPer];
+                const uint32_t hsize = last ? w.cached_size : 0;
+#pragma unroll
+                for (uint32_t q = 0; q < kPer; q++) {
+                    const uint32_t h = threadIdx.x + q * kThreads;
+                    hc[q] = 0;
+                    hold[q] = 0;
+                    if (h < hsize) {
+                        hc[q] = w.hdec[h];
+                        if (hc[q]) {
                             w.hdec[h] = 0;
-                            dec_edge(a, rd, w.hval[h], c);
+                            hold[q] = dec_issue<N32>(a, w.hval[h], hc[q]);
                         }
                     }
                 }
+                if (c) dec_settle(a, rd, w.mid_eid[threadIdx.x], c, old);
+#pragma unroll
+                for (uint32_t q = 0; q < kPer; q++)
+                    if (hc[q]) dec_settle(a, rd, w.hval[threadIdx.x + q * kThreads], hc[q], hold[q]);
             });
         wk.decs += hit.decs;
         wk.hits += hit.hits;
@@ -416,13 +461,14 @@ __device__ void peel_tasks(const MspArgs &a, Smem &sm, const uint32_t *curr, uin
 // ---------------------------------------------------------------------------
 
 // Minimum support over the live entries of `list` (grid-wide atomicMin).
+template <bool N32>
 __device__ void list_min(const MspArgs &a, const uint32_t *list, uint32_t len, unsigned long long *out) {
     unsigned long long v = ~0ull;
     const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, gsz = gridDim.x * blockDim.x;
     for (uint32_t i = gtid; i < len; i += gsz) {
         const uint32_t e = list[i];
         if (a.enter[e] == 0) {
-            const unsigned long long s = sup_of(a, e);
+            const unsigned long long s = sup_of<N32>(a, e);
             v = s < v ? s : v;
         }
     }
@@ -471,6 +517,7 @@ __device__ void compute_two_hop(const MspArgs &a) {
 // the persistent kernel
 // ---------------------------------------------------------------------------
 
+template <bool N32>
 __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
@@ -497,11 +544,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
         // ------------------------------------------------ level transition
         if (s->len[r % 3] == 0) {
             // T1: min over the near bucket (min_sup was reset in the last sub-round)
-            list_min(a, a.near_a, s->near_ctr[nsel], &s->min_sup);
+            list_min<N32>(a, a.near_a, s->near_ctr[nsel], &s->min_sup);
             if (!barrier(a, sm)) return;
             if (s->min_sup == ~0ull) {
                 // T2: near is dry -> split the far bucket
-                list_min(a, a.far_a, s->far_len, &s->far_min);
+                list_min<N32>(a, a.far_a, s->far_len, &s->far_min);
                 if (!barrier(a, sm)) return;
                 const unsigned long long lo = s->far_min;
                 if (lo == ~0ull) break;  // nothing left
@@ -509,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
                 for (uint32_t i = gtid; i < s->far_len; i += gsz) {
                     const uint32_t e = a.far_a[i];
                     if (a.enter[e] != 0) continue;
-                    if (sup_of(a, e) < hi) a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
+                    if (sup_of<N32>(a, e) < hi) a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
                     else a.far_b[atomicAdd(&s->far2_len, 1u)] = e;
                 }
                 if (!barrier(a, sm)) return;
@@ -539,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
             for (uint32_t i = gtid; i < near_len; i += gsz) {
                 const uint32_t e = a.near_a[i];
                 if (a.enter[e] != 0) continue;
-                if (sup_of(a, e) == L) {
+                if (sup_of<N32>(a, e) == L) {
                     a.enter[e] = r;
                     a.result[e] = (uint32_t)L;
                     front[atomicAdd(&s->len[r % 3], 1u)] = e;
@@ -612,10 +659,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
             s->subrounds++;
         }
         if (curr_len <= a.local_plan)
-            peel_tasks(a, sm, curr, curr_len, sm.lp_piv, sm.lp_anc, sm.lp_grain, sm.lp_total, sm.lp_start,
+            peel_tasks<N32>(a, sm, curr, curr_len, sm.lp_piv, sm.lp_anc, sm.lp_grain, sm.lp_total, sm.lp_start,
                        ntasks, &s->task_ctr[r % 3], rd, epoch, wk);
         else
-            peel_tasks(a, sm, curr, curr_len, a.pl_piv, a.pl_anc, a.pl_grain, a.pl_total, a.task_start,
+            peel_tasks<N32>(a, sm, curr, curr_len, a.pl_piv, a.pl_anc, a.pl_grain, a.pl_total, a.task_start,
                        ntasks, &s->task_ctr[r % 3], rd, epoch, wk);
         if (!barrier(a, sm)) return;
         if (a.trace && gtid == 0 && r < a.trace_cap) {
@@ -795,9 +842,10 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     }
     // cooperative persistent launch
     const size_t smem = sizeof(Smem);
-    C(cudaFuncSetAttribute(k_msp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const void *kfn = a.sup32 ? (const void *)k_msp<true> : (const void *)k_msp<false>;
+    C(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    C(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_msp, kThreads, smem));
+    C(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kThreads, smem));
     if (per_sm < 1) { release(); return bt_fail(BT_ERR_CUDA, "msp kernel does not fit on an SM"); }
     a.nblocks = (uint32_t)(ctx->sm_count * per_sm);
     // One cooperative peeling kernel at a time in this process: two grids that
@@ -810,7 +858,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
         coop.lock();
         void *params[] = {&a};
         cudaEventRecord(ctx->ev[4], st);
-        cudaError_t le = cudaLaunchCooperativeKernel((void *)k_msp, dim3(a.nblocks), dim3(kThreads), params, smem, st);
+        cudaError_t le = cudaLaunchCooperativeKernel(kfn, dim3(a.nblocks), dim3(kThreads), params, smem, st);
         if (le == cudaSuccess) le = cudaGetLastError();
         if (le != cudaSuccess) {
             coop.unlock();
