@@ -28,6 +28,7 @@
  */
 #include <omp.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -336,10 +337,16 @@ typedef struct {
     uint32_t *next;
     uint64_t next_len;
     uint64_t level;
+    /* table mode only: the "low" list of live edges with support < low_bound
+     * (see og_msp); NULL in merge mode */
+    uint32_t *low;
+    uint64_t low_len, low_bound;
 } og_peel;
 
 /* update_edge_support, cpu_bitruss.cpp:302-324: decrement, push the edge to
- * the next frontier when the old value was level+1, clamp at level. */
+ * the next frontier when the old value was level+1, clamp at level.  In table
+ * mode a decrement that takes the edge below low_bound also appends it to the
+ * low list (low_bound > level, so that decrement is never clamped). */
 static inline void og_dec(og_peel *p, uint32_t e) {
     uint64_t old;
 #pragma omp atomic capture
@@ -354,6 +361,12 @@ static inline void og_dec(og_peel *p, uint32_t e) {
     if (old <= p->level) {
 #pragma omp atomic
         p->sup[e]++;
+    }
+    if (p->low && old == p->low_bound) {
+        uint64_t slot;
+#pragma omp atomic capture
+        slot = p->low_len++;
+        p->low[slot] = e;
     }
 }
 
@@ -419,41 +432,88 @@ static void og_peel_edge_merge(const og_graph *g, og_peel *p, const uint32_t *de
     }
 }
 
+/* Two-hop sums of the current rows: two_hop[x] = sum of deg[y], y in N(x).
+ * Rows change only at a compression, so this is recomputed after each. */
+static void og_two_hop(const og_graph *g, const uint32_t *deg, const uint32_t *nbr,
+                       uint64_t *two_hop) {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (uint32_t x = 0; x < g->n; x++) {
+        uint64_t s = 0;
+        for (uint32_t i = 0; i < deg[x]; i++) s += deg[nbr[g->offsets[x] + i]];
+        two_hop[x] = s;
+    }
+}
+
+/* Slot of y in a sorted row of length d, or -1. */
+static inline int64_t og_find(const uint32_t *row, uint32_t d, uint32_t y) {
+    uint32_t lo = 0, hi = d;
+    while (lo < hi) {
+        uint32_t md = lo + ((hi - lo) >> 1);
+        if (row[md] < y) lo = md + 1;
+        else hi = md;
+    }
+    return lo < d && row[lo] == y ? (int64_t)lo : -1;
+}
+
 /*
- * Same butterflies as og_peel_edge_merge, found with a per-thread position
- * table: pos[x] = 1 + slot of x in the row of the anchor endpoint.  The side
- * whose two-hop neighbourhood is smaller is walked.  Every butterfly of uv is
- * visited exactly once either way, so the decrements are the same.
+ * Same butterflies as og_peel_edge_merge, found from the endpoint whose
+ * two-hop sum is smaller (the pivot): each y in N(mid), mid in N(pivot), is
+ * looked up in the row of the other endpoint (the anchor).  The lookup uses
+ * a per-thread position table, pos[x] = 1 + slot of x in the anchor's row,
+ * unless the anchor's row is long next to the probes (then filling the table
+ * would cost more than the walk), in which case it is a binary search of the
+ * sorted row.  A mid whose row is much longer than the anchor's is
+ * intersected the other way round (the anchor's row walked, each y searched
+ * in mid's sorted row).  Every butterfly of uv is visited exactly once either
+ * way, so the decrements are the same.
  */
 static void og_peel_edge_table(const og_graph *g, og_peel *p, const uint32_t *deg,
-                               const uint32_t *nbr, const uint32_t *eid, uint32_t uv,
-                               int exact, uint32_t *pos) {
+                               const uint32_t *nbr, const uint32_t *eid, const uint64_t *two_hop,
+                               uint32_t uv, int exact, uint32_t *pos) {
     uint32_t u = g->edges[2 * (uint64_t)uv], v = g->edges[2 * (uint64_t)uv + 1];
-    uint64_t cost_v = 0, cost_u = 0;
-    for (uint32_t i = 0; i < deg[v]; i++) cost_v += deg[nbr[g->offsets[v] + i]];
-    for (uint32_t i = 0; i < deg[u]; i++) cost_u += deg[nbr[g->offsets[u] + i]];
+    uint64_t cost_v = two_hop[v], cost_u = two_hop[u];
     /* walk: iterate mid in N(piv)\anchor, probe N(mid) against N(anchor) */
     uint32_t piv = cost_v <= cost_u ? v : u;
     uint32_t anc = piv == v ? u : v;
-    for (uint32_t i = 0; i < deg[anc]; i++) pos[nbr[g->offsets[anc] + i]] = i + 1;
+    uint64_t probes = piv == v ? cost_v : cost_u;
+    const uint32_t *arow = nbr + g->offsets[anc];
+    const uint32_t ad = deg[anc];
+    const int table = (uint64_t)ad <= 32 * probes;
+    if (table)
+        for (uint32_t i = 0; i < ad; i++) pos[arow[i]] = i + 1;
     for (uint32_t x = 0; x < deg[piv]; x++) {
         uint32_t mid = nbr[g->offsets[piv] + x];
         if (mid == anc) continue;
         uint32_t e_pm = eid[g->offsets[piv] + x];
         if (p->processed[e_pm]) continue;
-        for (uint32_t j = 0; j < deg[mid]; j++) {
-            uint32_t y = nbr[g->offsets[mid] + j];
-            uint32_t k = pos[y];
-            if (!k || y == piv) continue;
-            uint32_t e_my = eid[g->offsets[mid] + j];
-            uint32_t e_ay = eid[g->offsets[anc] + k - 1];
+        const uint32_t *mrow = nbr + g->offsets[mid];
+        const uint32_t md = deg[mid];
+        /* a mid row much longer than the anchor's is intersected the other
+         * way: each y of the anchor's row is looked up in mid's sorted row */
+        const int reverse = (uint64_t)md > 16 * (uint64_t)ad;
+        const uint32_t len = reverse ? ad : md;
+        for (uint32_t j = 0; j < len; j++) {
+            uint32_t y = reverse ? arow[j] : mrow[j];
+            if (y == piv) continue;
+            int64_t jm, ka;
+            if (reverse) {
+                ka = j;
+                jm = og_find(mrow, md, y);
+            } else {
+                jm = j;
+                ka = table ? (int64_t)pos[y] - 1 : og_find(arow, ad, y);
+            }
+            if (jm < 0 || ka < 0) continue;
+            uint32_t e_my = eid[g->offsets[mid] + (uint64_t)jm];
+            uint32_t e_ay = eid[g->offsets[anc] + (uint64_t)ka];
             if (p->processed[e_ay] || p->processed[e_my]) continue;
             /* name the edges as the reference does: w on u's side, x on v's */
             if (piv == v) og_rule(p, uv, e_pm, e_my, e_ay, exact); /* mid=w, y=x */
             else og_rule(p, uv, e_ay, e_my, e_pm, exact);          /* mid=x, y=w */
         }
     }
-    for (uint32_t i = 0; i < deg[anc]; i++) pos[nbr[g->offsets[anc] + i]] = 0;
+    if (table)
+        for (uint32_t i = 0; i < ad; i++) pos[arow[i]] = 0;
 }
 
 /* ccompress_graph, cpu_bitruss.cpp:527-557: keep only edges with sup > level. */
@@ -520,40 +580,107 @@ uint64_t og_msp(const og_graph *g, int threads, uint64_t *sup, int mode, uint64_
         else alive[alive_len++] = (uint32_t)e;
     }
 
+    /* Table mode finds each level's frontier without scanning every live
+     * edge (the reference scans all m edges per level, which is what makes a
+     * 20M-edge graph with ~10^5 levels take hours).  The live edges are split
+     * into a "low" list (support < low_bound) and a "high" list (the rest,
+     * `alive`).  Supports only fall, and og_dec appends an edge to low when a
+     * decrement takes it below low_bound, so every live edge with support
+     * below low_bound is in low.  Hence when low holds a live edge the
+     * smallest live support is in low; otherwise the high list is split again
+     * at its minimum + width (width adapted to keep low near 2^16 entries).
+     * Low may hold processed entries; they are dropped as they are met.
+     * Levels with an empty frontier change nothing and are skipped.  The
+     * n-sized position tables of the threads are allocated once. */
+    uint32_t *low = NULL, **pos_of = NULL;
+    uint64_t *two_hop = NULL;
+    uint64_t width = 1;
+    int nth = 1;
+    p.low = NULL;
+    p.low_len = 0;
+    p.low_bound = 0;
+    if (table) {
+        low = malloc(sizeof(uint32_t) * (m ? m : 1));
+        p.low = low;
+        nth = omp_get_max_threads();
+        pos_of = malloc(sizeof(uint32_t *) * (size_t)nth);
+        for (int t = 0; t < nth; t++) pos_of[t] = calloc(g->n ? g->n : 1, sizeof(uint32_t));
+        two_hop = malloc(sizeof(uint64_t) * (g->n ? g->n : 1));
+        og_two_hop(g, deg, nbr, two_hop);
+    }
+    const uint64_t low_target = 1u << 16;
+
     uint64_t level = 1, live = m, last = 0;
     const double t_start = omp_get_wtime();
     int expired = 0;
+    /* OG_MSP_PROGRESS=1: a progress line on stderr every 20,000 sub-rounds */
+    const int progress = getenv("OG_MSP_PROGRESS") != NULL;
     while (edge_num > 0 && !expired) {
-        if (table) {
-            /* levels with an empty frontier change nothing: jump to the
-             * smallest live support */
-            uint64_t lo = UINT64_MAX;
-            for (uint64_t i = 0; i < alive_len; i++)
-                if (sup[alive[i]] < lo) lo = sup[alive[i]];
-            if (lo > level) level = lo;
-        }
-        p.level = level;
-        /* scan_edge, cpu_bitruss.cpp:285-299 */
         uint64_t curr_len = 0;
-        for (uint64_t i = 0; i < alive_len; i++) {
-            uint32_t e = alive[i];
-            if (sup[e] == level) { p.in_curr[e] = 1; curr[curr_len++] = e; }
+        if (table) {
+            uint64_t lo = UINT64_MAX;
+            for (uint64_t i = 0; i < p.low_len; i++) {
+                uint32_t e = low[i];
+                if (!p.processed[e] && sup[e] < lo) lo = sup[e];
+            }
+            if (lo == UINT64_MAX) {
+                /* low is dry: split the high list at its minimum + width */
+                for (uint64_t i = 0; i < alive_len; i++) {
+                    uint32_t e = alive[i];
+                    if (!p.processed[e] && sup[e] < lo) lo = sup[e];
+                }
+                if (lo == UINT64_MAX) break; /* defensive: edge_num > 0 implies a live edge */
+                p.low_bound = lo + width;
+                p.low_len = 0;
+                uint64_t k = 0;
+                for (uint64_t i = 0; i < alive_len; i++) {
+                    uint32_t e = alive[i];
+                    if (p.processed[e]) continue;
+                    if (sup[e] < p.low_bound) low[p.low_len++] = e;
+                    else alive[k++] = e;
+                }
+                alive_len = k;
+                if (p.low_len > 4 * low_target && width > 1) width >>= 1;
+                else if (p.low_len < low_target / 4) width <<= 1;
+            }
+            level = lo; /* live supports never fall below the last level */
+            p.level = level;
+            /* the frontier: live low edges with support == level; the other
+             * live low edges stay */
+            uint64_t k = 0;
+            for (uint64_t i = 0; i < p.low_len; i++) {
+                uint32_t e = low[i];
+                if (p.processed[e]) continue;
+                if (sup[e] == level && !p.in_curr[e]) { p.in_curr[e] = 1; curr[curr_len++] = e; }
+                else if (sup[e] != level) low[k++] = e;
+            }
+            p.low_len = k;
+        } else {
+            p.level = level;
+            /* scan_edge, cpu_bitruss.cpp:285-299 */
+            for (uint64_t i = 0; i < alive_len; i++) {
+                uint32_t e = alive[i];
+                if (sup[e] == level) { p.in_curr[e] = 1; curr[curr_len++] = e; }
+            }
         }
         if (curr_len) last = level;
         while (curr_len) {
             edge_num -= (int64_t)curr_len;
             peeled += curr_len;
             subrounds++;
+            if (progress && subrounds % 20000 == 0)
+                fprintf(stderr, "og_msp: %llu sub-rounds, level %llu, %lld edges left, %.0f s\n",
+                        (unsigned long long)subrounds, (unsigned long long)level,
+                        (long long)edge_num, omp_get_wtime() - t_start);
             p.next_len = 0;
 #pragma omp parallel
             {
-                uint32_t *pos = table ? calloc(g->n ? g->n : 1, sizeof(uint32_t)) : NULL;
+                uint32_t *pos = table ? pos_of[omp_get_thread_num()] : NULL;
 #pragma omp for schedule(dynamic, 1)
                 for (uint64_t i = 0; i < curr_len; i++) {
-                    if (table) og_peel_edge_table(g, &p, deg, nbr, eid, curr[i], exact, pos);
+                    if (table) og_peel_edge_table(g, &p, deg, nbr, eid, two_hop, curr[i], exact, pos);
                     else og_peel_edge_merge(g, &p, deg, nbr, eid, curr[i], exact);
                 }
-                free(pos);
             }
             for (uint64_t i = 0; i < curr_len; i++) {
                 p.processed[curr[i]] = 1;
@@ -569,17 +696,26 @@ uint64_t og_msp(const og_graph *g, int threads, uint64_t *sup, int mode, uint64_
                 break;
             }
         }
-        uint64_t k = 0;
-        for (uint64_t i = 0; i < alive_len; i++)
-            if (!p.processed[alive[i]]) alive[k++] = alive[i];
-        alive_len = k;
+        if (!table) {
+            uint64_t k = 0;
+            for (uint64_t i = 0; i < alive_len; i++)
+                if (!p.processed[alive[i]]) alive[k++] = alive[i];
+            alive_len = k;
+        }
         if ((double)edge_num <= (double)live * 0.5 && (double)live >= (double)m * 0.1) {
             live = og_compress(g, sup, level, deg, nbr, eid);
             compressions++;
+            if (table) og_two_hop(g, deg, nbr, two_hop);
         }
         level++;
     }
     free(alive);
+    free(low);
+    free(two_hop);
+    if (pos_of) {
+        for (int t = 0; t < nth; t++) free(pos_of[t]);
+        free(pos_of);
+    }
     if (stats) {
         stats[0] = last;
         stats[1] = subrounds;

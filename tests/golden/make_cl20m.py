@@ -40,8 +40,8 @@ def main():
                 "ebfc_seconds": round(time.time() - t, 1)})
     if args.msp:
         t = time.time()
-        res, levels, _ = O.msp(g, args.threads, O.MSP_TABLE, sup)
-        out.update({"levels": int(levels),
+        res, levels, st = O.msp(g, args.threads, O.MSP_TABLE, sup)
+        out.update({"levels": int(levels), "subrounds": int(st[1]),
                     "msp_sha256": hashlib.sha256(res.astype("<u4").tobytes()).hexdigest(),
                     "msp_seconds": round(time.time() - t, 1)})
     with open(path, "w") as f:

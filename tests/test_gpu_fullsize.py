@@ -37,3 +37,5 @@ def test_cl20m_counts_and_decomposition(engine, gpu_ctx):
     if "msp_sha256" in want:
         assert hashlib.sha256(b.astype("<u4").tobytes()).hexdigest() == want["msp_sha256"]
         assert levels == want["levels"]
+    if "subrounds" in want:
+        assert gpu_ctx.stats()[1] == want["subrounds"]

@@ -147,3 +147,26 @@ def test_oracle_planted_mistake_is_caught(oracle_mod):
     planted[np.argmax(sup)] += 3
     res, _, _ = oracle_mod.msp(g, 1, oracle_mod.MSP_REF, planted)
     assert not np.array_equal(res, gd["msp"])
+
+
+@pytest.mark.parametrize("shape", ["cl50k", "hub"])
+def test_table_form_equals_merge_form(oracle_mod, shape):
+    """The table form of og_msp (position tables or binary search, reverse
+    intersection for long mid rows, low-list level discovery) visits the same
+    butterflies as the merge form, which follows the reference line by line:
+    identical results, levels and sub-rounds.  The hub-skewed graph has mid
+    rows far longer than most anchors and anchors far longer than most walks,
+    so every lookup path of the table form runs."""
+    from gpu_bitruss_gb300 import gen
+    if shape == "hub":
+        u, v = gen.hub_skew(nu=300, nv=20_000, m=40_000, gamma_u=1.8, cap_u=8_000, seed=11)
+    else:
+        u, v = gen.by_name(shape)
+    g = oracle_mod.build_csr(u, v)
+    sup, _ = oracle_mod.ebfc(g, 4)
+    for ref_mode, table_mode in ((oracle_mod.MSP_REF, oracle_mod.MSP_TABLE),
+                                 (oracle_mod.MSP_EXACT, oracle_mod.MSP_TABLE_EXACT)):
+        a, la, sa = oracle_mod.msp(g, 4, ref_mode, sup)
+        b, lb, sb = oracle_mod.msp(g, 4, table_mode, sup)
+        np.testing.assert_array_equal(a, b)
+        assert la == lb and sa[1] == sb[1]
