@@ -43,7 +43,8 @@ def main():
         res, levels, st = O.msp(g, args.threads, O.MSP_TABLE, sup)
         out.update({"levels": int(levels), "subrounds": int(st[1]),
                     "msp_sha256": hashlib.sha256(res.astype("<u4").tobytes()).hexdigest(),
-                    "msp_seconds": round(time.time() - t, 1)})
+                    "msp_seconds": round(time.time() - t, 1),
+                    "msp_threads": args.threads or os.cpu_count()})
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
     print(json.dumps(out))
