@@ -312,19 +312,21 @@ struct MspHit {
     bool piv_is_v;
     unsigned long long decs = 0, hits = 0;
     struct State {
-        uint32_t kslot, e_my, e_ay, ah, en_my, en_ay;
-        // old supports of the global decrements this hit has in flight, 0 for
-        // none (a decremented edge's old support is at least 1: an edge loses
-        // at most one support per butterfly it is in)
-        SupWord<N32> old_my, old_ay;
+        uint32_t kslot, e_my, e_ay, ah;
+        // After load(): the stamps of e_my and e_ay.  After apply(): the old
+        // supports of the global decrements the hit has in flight, 0 for none
+        // (a decremented edge's old support is at least 1: an edge loses at
+        // most one support per butterfly it is in).  One pair of fields for
+        // both keeps a lane's four hits within the register budget.
+        SupWord<N32> x_my, x_ay;
     };
     __device__ __forceinline__ void load(State &s, uint32_t kk, uint32_t e_my, uint32_t ah) const {
         s.kslot = kk & ~(uint32_t)bt::kRevHit;
         s.e_my = e_my;
         s.ah = ah;
         s.e_ay = bt::walk_anchor_edge(w, ah);
-        s.en_my = a.enter[e_my];
-        s.en_ay = a.enter[s.e_ay];
+        s.x_my = a.enter[e_my];
+        s.x_ay = a.enter[s.e_ay];
     }
     // The rule for one hit.  Pivot-side and staged anchor-side decrements are
     // summed in shared memory; the others are issued here and settled by
@@ -332,10 +334,11 @@ struct MspHit {
     __device__ __forceinline__ void apply(State &s) {
         const uint32_t r = rd.r;
         hits++;  // a butterfly visited (the reference's intersection hit)
-        s.old_my = s.old_ay = 0;
-        if (is_done(s.en_ay, r) || is_done(s.en_my, r)) return;
+        const uint32_t en_my = (uint32_t)s.x_my, en_ay = (uint32_t)s.x_ay;
+        s.x_my = s.x_ay = 0;
+        if (is_done(en_ay, r) || is_done(en_my, r)) return;
         const uint32_t e_pm = w.mid_eid[s.kslot];
-        const bool c_pm = w.pm_curr[s.kslot], c_my = s.en_my == r, c_ay = s.en_ay == r;
+        const bool c_pm = w.pm_curr[s.kslot], c_my = en_my == r, c_ay = en_ay == r;
         // name the edges as the reference does: w on u's side, x on v's
         uint32_t wv, ux;
         bool cwv, cux;
@@ -348,15 +351,15 @@ struct MspHit {
         const bool dec_ay = piv_is_v ? d_ux : d_wv;
         decs += (uint32_t)dec_pm + (uint32_t)d_wx + (uint32_t)dec_ay;
         if (dec_pm) atomicAdd(&w.slot_dec[s.kslot], 1u);
-        if (d_wx) s.old_my = dec_issue<N32>(a, s.e_my, 1);
+        if (d_wx) s.x_my = dec_issue<N32>(a, s.e_my, 1);
         if (dec_ay) {
             if (w.cached_size) atomicAdd(&w.hdec[s.ah], 1u);
-            else s.old_ay = dec_issue<N32>(a, s.e_ay, 1);
+            else s.x_ay = dec_issue<N32>(a, s.e_ay, 1);
         }
     }
     __device__ __forceinline__ void settle(const State &s) const {
-        if (s.old_my) dec_settle(a, rd, s.e_my, 1, s.old_my);
-        if (s.old_ay) dec_settle(a, rd, s.e_ay, 1, s.old_ay);
+        if (s.x_my) dec_settle(a, rd, s.e_my, 1, s.x_my);
+        if (s.x_ay) dec_settle(a, rd, s.e_ay, 1, s.x_ay);
     }
 };
 
