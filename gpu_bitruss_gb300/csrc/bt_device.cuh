@@ -313,8 +313,8 @@ __device__ inline uint32_t warp_find_slot(const uint32_t *pre, uint32_t d, uint3
 // on_hit.apply(state) for each, then on_hit.settle(state) for each.  k =
 // slice slot of mid (| kRevHit for a reverse hit), e_my = the edge id
 // (mid, y), a = the anchor's answer for y (walk_lookup's convention: a hash
-// slot when anc is staged, else the edge id), then on_hit.settle(state) for
-// each (results of atomics that apply issued).  slice_done(cl, last) runs
+// slot when anc is staged, else the edge id).  settle acts on the results of
+// atomics that apply issued.  slice_done(cl, last) runs
 // (block-uniform) after each slice's last hit; last marks the final slice.
 template <class PrepSlot, class OnHit, class SliceDone>
 __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre, Walk &w, uint32_t piv,

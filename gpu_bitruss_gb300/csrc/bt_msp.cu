@@ -167,11 +167,6 @@ struct Round {
     uint32_t *near_list, *near_len;
 };
 
-// Subtract k from sup[e].  The decrement that takes it from above L to L or
-// below puts e in the next frontier (stamp r+1, result L): the reference's
-// clamp at L (update_edge_support, bitruss_msp.cu:110-123) then only matters
-// for the value it is processed with, which is L.  A decrement crossing hi
-// appends e to the near bucket.
 // The kernel is compiled twice: N32 = every working support fits 32 bits
 // (4-byte supports and atomics), else 64-bit supports.
 template <bool N32>
@@ -183,6 +178,11 @@ __device__ __forceinline__ unsigned long long sup_of(const MspArgs &a, uint32_t 
     else return a.sup[e];
 }
 
+// Subtract k from sup[e].  The decrement that takes it from above L to L or
+// below puts e in the next frontier (stamp r+1, result L): the reference's
+// clamp at L (update_edge_support, bitruss_msp.cu:110-123) then only matters
+// for the value it is processed with, which is L.  A decrement crossing hi
+// appends e to the near bucket.
 // A decrement is split in two so that a thread can have several in flight:
 // dec_issue sends the atomic and returns the old support (nothing waits for
 // it until the value is used), dec_settle acts on the crossings it shows.
