@@ -170,3 +170,31 @@ def test_table_form_equals_merge_form(oracle_mod, shape):
         b, lb, sb = oracle_mod.msp(g, 4, table_mode, sup)
         np.testing.assert_array_equal(a, b)
         assert la == lb and sa[1] == sb[1]
+
+
+@pytest.mark.parametrize("shape", ["cl50k", "hub"])
+def test_table_form_equals_reference_msp(oracle_mod, shape):
+    """Beyond the golden fixtures: the oracle's table form against the
+    reference's own CPU msp (c_bitruss_msp, built from its sources here; one
+    thread, where it is deterministic) on a 50k-edge power-law graph and a
+    hub-skewed graph -- per-edge results and the reference's level count."""
+    import os
+    import tempfile
+    from gpu_bitruss_gb300 import gen
+    O = oracle_mod
+    if not O.ref_available():
+        pytest.skip("reference CPU code not built on this host")
+    if shape == "hub":
+        u, v = gen.hub_skew(nu=300, nv=20_000, m=40_000, gamma_u=1.8, cap_u=8_000, seed=11)
+    else:
+        u, v = gen.by_name(shape)
+    with tempfile.TemporaryDirectory() as d:
+        txt, binp = os.path.join(d, "g.txt"), os.path.join(d, "g.bin")
+        gen.to_text(txt, u, v)
+        O.ref_convert(txt, binp)
+        out, log = O.ref_run(binp, "msp", 1, int(u.size))
+    g = O.build_csr(u, v)
+    sup, _ = O.ebfc(g, 4)
+    res, levels, _ = O.msp(g, 4, O.MSP_TABLE, sup)
+    np.testing.assert_array_equal(np.asarray(out, np.uint64), res)
+    assert levels == O.ref_log_levels(log)
