@@ -173,11 +173,12 @@ def test_table_form_equals_merge_form(oracle_mod, shape):
 
 
 @pytest.mark.parametrize("shape", ["cl50k", "hub"])
-def test_table_form_equals_reference_msp(oracle_mod, shape):
+def test_oracle_equals_reference_on_larger_graphs(oracle_mod, shape):
     """Beyond the golden fixtures: the oracle's table form against the
     reference's own CPU msp (c_bitruss_msp, built from its sources here; one
     thread, where it is deterministic) on a 50k-edge power-law graph and a
-    hub-skewed graph -- per-edge results and the reference's level count."""
+    hub-skewed graph -- per-edge results and the reference's level count; the
+    supports and butterfly counts (ebfc, bfc) and, on the hub graph, hidx."""
     import os
     import tempfile
     from gpu_bitruss_gb300 import gen
@@ -193,8 +194,16 @@ def test_table_form_equals_reference_msp(oracle_mod, shape):
         gen.to_text(txt, u, v)
         O.ref_convert(txt, binp)
         out, log = O.ref_run(binp, "msp", 1, int(u.size))
+        ref = {algo: O.ref_run(binp, algo, 1, int(u.size)) for algo in ("ebfc", "bfc")}
+        if shape == "hub":  # the reference's hidx takes minutes on cl50k, seconds here
+            ref["hidx"] = O.ref_run(binp, "hidx", 1, int(u.size))
     g = O.build_csr(u, v)
-    sup, _ = O.ebfc(g, 4)
+    sup, count = O.ebfc(g, 4)
     res, levels, _ = O.msp(g, 4, O.MSP_TABLE, sup)
     np.testing.assert_array_equal(np.asarray(out, np.uint64), res)
     assert levels == O.ref_log_levels(log)
+    np.testing.assert_array_equal(np.asarray(ref["ebfc"][0], np.uint64), sup)
+    assert O.ref_log_count(ref["ebfc"][1]) == count == O.ref_log_count(ref["bfc"][1])
+    if "hidx" in ref:
+        h, _ = O.hidx(g, 4, sup)
+        np.testing.assert_array_equal(np.asarray(ref["hidx"][0], np.uint64), h)
