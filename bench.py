@@ -7,28 +7,36 @@ Workload (default): the Chung-Lu power-law bipartite graph |U|=1,000,000,
 |V|=500,000, 20,000,000 unique edges, degree exponent 2.1 on both sides,
 degree cap 50,000, seed 2 (synthetic; see gpu_bitruss_gb300/gen.py).
 
-A step is one full msp decomposition of the resident graph through the C ABI
-(bt_msp: butterfly supports, then peeling to the bitruss number of every
-edge).  value = edges decomposed per second = m * K / (device time of the K
-timed steps), inputs resident in HBM.  Between timed steps L2 is flushed by
-writing a 512 MB buffer (and the graph arrays alone exceed the 129 MB L2).
+A step is one msp decomposition through the public C ABI: the graph's CSR
+from host memory to the device (bt_graph_upload), bt_msp (butterfly supports,
+then peeling to the bitruss number of every edge) and the m uint32 results
+back to host memory.  value = edges decomposed per second = m * K / (device
+time of bt_msp over the K timed steps, measured with CUDA events on the
+library's stream; the graph is resident in HBM when that region starts).
+Before every step L2 is flushed by writing a 512 MB buffer (and the graph
+arrays alone exceed the 129 MB L2).
 
-e2e: the same metric through the public API with host buffers: every step
-uploads the graph from host memory (H2D of offsets, degrees, neighbours, edge
-ids) and copies the m uint32 results back (D2H).
+e2e: the same metric over the wall time of the whole step (upload from
+pageable host memory: offsets, degrees, neighbours, edge ids; bt_msp; D2H of
+the m uint32 results).
 
-roofline: the peeling kernel k_msp (the dominant kernel); achieved = its
-algorithmic bytes (counted by the kernel: 8 B per pivot slot walked (neighbour
-+ edge id), 4 B per neighbour slot probed, 4 B per anchor slot staged, 8 B per
-butterfly found (two edge ids), 8 B per support decrement) / its CUDA-event
-time; peak = measured HBM copy bandwidth.
+roofline: the peeling kernel k_msp (the dominant kernel); achieved =
+algorithmic bytes / its CUDA-event time; peak = measured HBM copy bandwidth.
+The algorithmic bytes are the oracle's count for the workload when
+tests/golden/<workload>.json holds one (per peeled edge uv, u = U end, v = V
+end, at the start of its sub-round: 4 B per live neighbour of u, 8 B per live
+neighbour of v, 4 B per live neighbour of every live w in N(v) minus u; plus
+8 B per butterfly visited and 8 B per unit decrement).  The kernel's own
+count rides along: 4 B per row position probed (forward or reverse), 4 B per
+anchor slot staged, 8 B per butterfly found, and 4 or 8 B (the width of the
+working supports) per unit decrement.
 
 cpu_baseline / --impl reference: the CPU restatement of the reference's
 algorithm (oracle/bt_oracle.c, OpenMP, all host cores) on a bounded sample of
-the same graph: butterfly supports of the whole graph, then peeling for a
-fixed time budget (20 s); edges peeled / elapsed time.  Peeling takes the
-cheapest edges first, so the sample overstates the CPU's whole-run rate.
-Warm-up steps of the reference arm compute the supports only.
+the same graph, built by the oracle: butterfly supports of the whole graph,
+then peeling for a fixed time budget (20 s); edges peeled / elapsed time.
+Peeling takes the cheapest edges first, so the sample overstates the CPU's
+whole-run rate.  Warm-up steps of the reference arm compute the supports only.
 
 Batched workload (--workload batch<N>, e.g. batch256): the first N graphs of
 the 4,096-graph batch (gen.batch_graph: m log-uniform in [1e3, 2e6], Chung-Lu
@@ -149,20 +157,27 @@ class ClockSampler:
 
 
 def make_graph(workload: str):
+    """The workload's edge list (draw order) and its digest."""
     from gpu_bitruss_gb300 import gen
-    import gpu_bitruss_gb300 as bt
     u, v = gen.by_name(workload)
-    g = bt.Graph.from_edges(u, v)
-    return g, gen.digest(u, v)
+    return (u, v), gen.digest(u, v)
 
 
-def cpu_sample(g, threads: int, budget_s: float, peel: bool = True):
-    """Oracle (reference algorithm restated) on a bounded sample of the graph:
-    supports of the whole graph + peeling for budget_s seconds.  Peeling takes
-    the cheapest edges first, so this rate overstates the CPU's rate over a
-    whole decomposition."""
+def oracle_graph(edges):
+    """The reference CSR of the edge list, built by the oracle (the
+    reference's process_graph restated): the CPU arm maps none of this
+    engine's code."""
     from oracle import oracle as O
-    d = g.as_dict()
+    return O.build_csr(*edges)
+
+
+def cpu_sample(d: dict, threads: int, budget_s: float, peel: bool = True):
+    """Oracle (the reference's CPU msp restated) on a bounded sample of the
+    workload: butterfly supports of the whole graph, then peeling for
+    budget_s seconds.  Returns (edges peeled / elapsed s, edges peeled,
+    elapsed s).  Peeling takes the cheapest edges first, so this rate
+    overstates the CPU's rate over a whole decomposition."""
+    from oracle import oracle as O
     t0 = time.perf_counter()
     sup, _ = O.ebfc(d, threads)
     peeled = 0
@@ -173,30 +188,48 @@ def cpu_sample(g, threads: int, budget_s: float, peel: bool = True):
     return peeled / dt, peeled, dt
 
 
+def golden_facts(workload: str) -> dict:
+    """Oracle facts of a full-size workload (tests/golden/<workload>.json)."""
+    p = os.path.join(ROOT, "tests", "golden", f"{workload}.json")
+    return json.load(open(p)) if os.path.exists(p) else {}
+
+
+CPU_SAMPLE_NOTE = ("bounded sample, not the same work as a GPU step: supports of the whole graph, "
+                   "then peeling for a fixed time; peeling takes the cheapest edges first, so the "
+                   "rate overstates the CPU's rate over a whole decomposition")
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    g, dig = make_graph(args.workload)
+    edges, dig = make_graph(args.workload)
+    d = oracle_graph(edges)
+    m = int(d["m"])
     vals = []
     for i in range(args.warmup + args.steps):
         # warm-up steps compute the supports only (threads and caches warm)
-        v, peeled, dt = cpu_sample(g, threads, args.cpu_budget, peel=i >= args.warmup)
+        v, peeled, dt = cpu_sample(d, threads, args.cpu_budget, peel=i >= args.warmup)
         if i >= args.warmup:
             vals.append((v, peeled, dt))
     tot_e = sum(p for _, p, _ in vals)
     tot_t = sum(t for _, _, t in vals)
     value = tot_e / tot_t
-    sample = (f"oracle port, {threads} threads: supports of all {g.m} edges + peeling for "
-              f"{args.cpu_budget:.0f} s; {vals[-1][1]} edges peeled per step")
+    facts = golden_facts(args.workload)
+    sample = (f"oracle port (the reference's CPU msp restated, table form), {threads} threads: "
+              f"supports of all {m} edges + peeling for {args.cpu_budget:.0f} s per step; "
+              f"{vals[-1][1]} edges peeled per step; {CPU_SAMPLE_NOTE}")
+    if facts.get("oracle_msp_s"):
+        sample += (f"; the oracle's full decomposition of this graph took {facts['oracle_msp_s']:.0f} s "
+                   f"on {facts.get('oracle_threads', '?')} x86 threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "edges/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * tot_t / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "uint64", "data": "synthetic",
         "config": {"workload": args.workload, "desc": WORKLOADS.get(args.workload, ""),
-                   "m": int(g.m), "graph_digest": dig, "parallelism": "replicas"},
+                   "m": m, "graph_digest": dig, "parallelism": "replicas"},
         "cpu_baseline": {"value": value, "unit": "edges/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -214,22 +247,42 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    g, dig = make_graph(args.workload)
-    m = int(g.m)
+    t_gen = time.perf_counter()
+    edges, dig = make_graph(args.workload)
+    g = bt.Graph.from_edges(*edges)
+    t_gen = time.perf_counter() - t_gen
+    m, n = int(g.m), int(g.n)
     ctx = bt.Context(local)
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
-    ctx.upload(g)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
+    out = np.zeros(max(m, 1), np.uint32)
+    # H2D per step: offsets, degrees, neighbours and edge ids of the host CSR
+    h2d = 4 * (n + 1) + 4 * n + 8 * m + 8 * m
+    d2h = 4 * m
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    # warm-up
+    def step():
+        """One step through the public API: the graph's CSR from host memory
+        to the device (bt_graph_upload), bt_msp (supports + peeling), the m
+        bitruss numbers back to host memory.  Returns (wall ms of the whole
+        step, device ms of bt_msp with the graph resident, device ms of the
+        peeling kernel)."""
+        with torch.cuda.stream(stream):
+            flush.fill_(1)  # L2 flush: 512 MB written between steps
+        stream.synchronize()
+        t0 = time.perf_counter()
+        ctx.upload(g)
+        ctx.msp(out=True, into=out)
+        wall = 1000 * (time.perf_counter() - t0)
+        return wall, ctx.phase_ms("total"), ctx.phase_ms("peel")
+
     for _ in range(args.warmup):
-        ctx.msp(out=False)
+        step()
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -237,49 +290,39 @@ def run_ours(args):
     time.sleep(0.3)
     barrier()
     torch.cuda.synchronize()
-    total_ms, peel_ms, work = 0.0, [], None
     launches0 = bt.kernel_launches()
+    walls, devs, peels = [], [], []
     for _ in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(1)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-        ctx.msp(out=False)
-        with torch.cuda.stream(stream):
-            e1.record(stream)
-        e1.synchronize()
-        total_ms += e0.elapsed_time(e1)
-        peel_ms.append(ctx.phase_ms("peel"))
-        st = ctx.stats()
-        work = st[8:17]
+        w, dv, pl = step()
+        walls.append(w)
+        devs.append(dv)
+        peels.append(pl)
     torch.cuda.synchronize()
-    launches = bt.kernel_launches() - launches0  # k_count, k_msp_init, k_two_hop, k_msp per step
     barrier()
+    launches = bt.kernel_launches() - launches0
     clk = clocks.stop()
     stats = ctx.stats()
-    t_max = max_over_ranks(total_ms, device=f"cuda:{local}")
+    dev_ms = sum(devs)
+    t_max = max_over_ranks(dev_ms, device=f"cuda:{local}")
+    e2e_max = max_over_ranks(sum(walls), device=f"cuda:{local}")
     value = world * m * args.steps / (t_max / 1000.0)
+    e2e_value = world * m * args.steps / (e2e_max / 1000.0)
 
-    # e2e through the public API: H2D upload + msp + D2H of the results
-    out = np.zeros(m, np.uint32)
-    h2d = 4 * (g.n + 1) + 4 * g.n + 8 * m + 8 * m
-    e2e_ms = 0.0
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.upload(g)
-        b, _ = ctx.msp(out=True)
-        e2e_ms += 1000 * (time.perf_counter() - t0)
-    e2e_value = world * m * args.steps / (e2e_ms / 1000.0)
-
-    # roofline of k_msp
-    mids, probes, anchor, hits, decs = work[:5]
-    alg_bytes = 4 * probes + 4 * anchor + 8 * hits + 8 * decs
-    t_peel = statistics.median(peel_ms) / 1000.0
+    # roofline of k_msp, the peeling kernel
+    work = stats[8:20]
+    tasks, probes, anchor, hits, decs = work[:5]
+    dec_bytes = stats[17] or 8  # width of the working supports (4 or 8 bytes)
+    kernel_bytes = 4 * probes + 4 * anchor + 8 * hits + dec_bytes * decs
+    t_peel = statistics.median(peels) / 1000.0
+    facts = golden_facts(args.workload)
+    alg_bytes = facts.get("msp_alg_bytes")
+    alg_src = "oracle-counted algorithmic bytes (tests/golden)" if alg_bytes else "kernel-counted bytes"
+    if not alg_bytes:
+        alg_bytes = kernel_bytes
     achieved = alg_bytes / t_peel / 1e9
     peak, peak_kind = load_peaks()
     traffic = load_traffic(args.workload)
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
 
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world,
@@ -287,32 +330,40 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "uint64",
         "data": "synthetic",
         "config": {"workload": args.workload, "desc": WORKLOADS.get(args.workload, ""),
-                   "m": m, "n": int(g.n), "graph_digest": dig, "parallelism": "replicas",
-                   "l2": "512 MB flush between timed steps; graph arrays > L2",
+                   "m": m, "n": n, "graph_digest": dig, "parallelism": "replicas",
+                   "l2": "512 MB flush before every step; graph arrays > L2",
+                   "step": "upload from host + bt_msp (supports + peeling) + results to host; "
+                           "value times bt_msp on the device with the graph resident",
                    "levels": stats[0], "subrounds": stats[1], "tasks": stats[3],
-                   "peel_ms": statistics.median(peel_ms), "ebfc_ms": ctx.phase_ms("ebfc"),
-                   "kernel_phase_ms": {"level_transitions": work[6] / 1e6, "peel": work[7] / 1e6,
-                                       "finalize": work[8] / 1e6},
+                   "peel_ms": statistics.median(peels), "step_device_ms": statistics.median(devs),
+                   "step_wall_ms": statistics.median(walls), "gen_s": round(t_gen, 1),
+                   "kernel_phase_ms": {"level_transitions": work[6] / 1e6, "peel": work[7] / 1e6},
                    "cta_ms_by_step": dict(zip(["task", "stage", "slice", "probe", "hits", "flush",
                                                "barrier", "other"],
-                                              [round(c / 2.07e6, 1) for c in stats[20:28]]))},
+                                              [round(c / (mhz * 1e3), 1) for c in stats[20:28]]))},
         "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(4 * m)},
+                "d2h_bytes_per_step": int(d2h),
+                "note": "every step: CSR from pageable host memory, bt_msp, bitruss numbers to host"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "k_msp",
-                     "algorithmic_bytes": int(alg_bytes),
-                     "work": {"tasks": mids, "probes": probes, "anchor_slots": anchor,
-                              "butterflies": hits, "decrements": decs}},
+                     "algorithmic_bytes": int(alg_bytes), "algorithmic_bytes_source": alg_src,
+                     "kernel_counted": {"bytes": int(kernel_bytes),
+                                        "achieved": kernel_bytes / t_peel / 1e9,
+                                        "frac": kernel_bytes / t_peel / 1e9 / peak,
+                                        "tasks": tasks, "probes": probes, "anchor_slots": anchor,
+                                        "butterflies": hits, "decrements": decs,
+                                        "decrement_bytes": dec_bytes}},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu:
-        v, peeled, dt = cpu_sample(g, os.cpu_count() or 1, args.cpu_budget)
+        d = oracle_graph(edges)
+        v, peeled, dt = cpu_sample(d, os.cpu_count() or 1, args.cpu_budget)
         line["cpu_baseline"] = {
             "value": v, "unit": "edges/s", "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"oracle port: supports of all {m} edges + peeling for "
-                      f"{args.cpu_budget:.0f} s ({peeled} edges peeled in {dt:.1f} s)"}
+                      f"{args.cpu_budget:.0f} s ({peeled} edges peeled in {dt:.1f} s); {CPU_SAMPLE_NOTE}"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -289,9 +289,16 @@ class Context:
         _check(load().bt_hidx(self._c, _ptr(b) if m else None, C.byref(r)), "g_bitruss_hindex")
         return b, r.value
 
-    def msp(self, exact: bool = False, out: bool = True):
+    def msp(self, exact: bool = False, out: bool = True, into: np.ndarray | None = None):
+        """Bitruss numbers of the resident graph (into `into` when given,
+        a uint32 array of at least m entries) and the level count."""
         m = self.graph.m
-        b = np.zeros(m, np.uint32) if out else None
+        if into is not None:
+            if into.dtype != np.uint32 or into.size < m or not into.flags.c_contiguous:
+                raise ValueError("into must be a contiguous uint32 array of at least m entries")
+            b = into
+        else:
+            b = np.zeros(m, np.uint32) if out else None
         lv = C.c_uint32()
         f = load().bt_msp_exact if exact else load().bt_msp
         _check(f(self._c, _ptr(b) if m else None, C.byref(lv)), "bitruss_msp")
@@ -347,7 +354,8 @@ class Context:
         """[levels, sub-rounds, compressions, tasks, hidx rounds, non-empty
         levels, bucket splits, -, peel tasks run, probes, anchor slots,
         butterflies found, decrements, m, ns in level transitions, ns in
-        peel phases, ns in finalize phases, -, -, -, then SM cycles per CTA
+        peel phases, ns in finalize phases, bytes per working support (4 or 8),
+        -, -, then SM cycles per CTA
         of the peeling kernel by step: task, stage, slice, probe, hits, flush,
         barrier, other]"""
         a = (C.c_uint64 * 28)()

@@ -920,6 +920,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     ctx->work[6] = h.ph_ns[0];
     ctx->work[7] = h.ph_ns[1];
     ctx->work[8] = 0;
+    ctx->work[9] = a.sup32 ? 4 : 8;  // bytes per working support (and per decrement)
     for (int q = 0; q < 8; q++) ctx->prof[q] = h.prof[q] / (a.nblocks ? a.nblocks : 1);
     ctx->last_result = 2;
     if (levels) *levels = (uint32_t)h.last_level;

@@ -20,12 +20,19 @@
 //
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (the host-side name of a __device__ array is only a
-// stand-in); that set-up runs once per device, with the device current, and
-// that first call should come before any stream capture.
+// stand-in); that set-up runs once per device and context, with the device
+// current, and that first call should come before any stream capture.  The
+// address is cached together with the CUDA context it belongs to: after the
+// caller resets the device (cudaDeviceReset) the next call sees a new context
+// and looks the address up again, so it never launches on a stale pointer.
+//
+// The call makes `device` current only for its own work and restores the
+// caller's current device before it returns, on every path.
 //
 // Arithmetic: the vertex-priority count of the reference's bfc_kernel
 // (src/bfc/bfc_vpp.cu:33-107) on the reference CSR layout (rows sorted by
 // vertex id, priority p(x) = (degree, id) tested per neighbour).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -43,8 +50,39 @@ constexpr int kThreadsNA = 512;
 __device__ __align__(256) uint32_t g_noalloc_scratch[kScratchWords + kCounterWords];
 
 uint32_t *g_scratch_addr[kMaxDevices];
-bool g_scratch_ready[kMaxDevices];
+CUcontext g_scratch_ctx[kMaxDevices];  // context the cached address belongs to
 std::mutex g_scratch_mutex;
+
+// The caller's current device, put back when the scope ends.
+struct DeviceGuard {
+    int saved = -1;
+    DeviceGuard() {
+        if (cudaGetDevice(&saved) != cudaSuccess) saved = -1;
+    }
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+    DeviceGuard(const DeviceGuard &) = delete;
+    DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+
+// The current CUDA context, through the driver entry point the runtime hands
+// out (the library does not link the driver library itself).
+bt_status current_context(CUcontext *out) {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    static GetCurrent fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+            return bt_fail(BT_ERR_CUDA, "cuCtxGetCurrent is not available from the CUDA driver");
+        fn = reinterpret_cast<GetCurrent>(p);
+    }
+    *out = nullptr;
+    if (fn(out) != CUDA_SUCCESS || !*out) return bt_fail(BT_ERR_CUDA, "no current CUDA context");
+    return BT_OK;
+}
 
 __device__ __forceinline__ bool higher(const uint32_t *off, uint32_t a, uint32_t b) {
     const uint32_t da = off[a + 1] - off[a], db = off[b + 1] - off[b];
@@ -97,16 +135,20 @@ __global__ void __launch_bounds__(kThreadsNA) k_bfc_noalloc(uint32_t n, const ui
     }
 }
 
-// Device address of the scratch array on the current device (set-up once).
+// Device address of the scratch array on the current device: looked up once
+// per device and context (`device` is current: cudaSetDevice has created or
+// bound its primary context).
 bt_status scratch_address(int device, uint32_t **out) {
     if (device < 0 || device >= kMaxDevices) return bt_fail(BT_ERR_INVALID, "device index out of range");
+    CUcontext cur = nullptr;
+    BT_TRY(current_context(&cur));
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_ready[device]) {
+    if (g_scratch_ctx[device] != cur) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return bt_cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
         g_scratch_addr[device] = static_cast<uint32_t *>(p);
-        g_scratch_ready[device] = true;
+        g_scratch_ctx[device] = cur;
     }
     *out = g_scratch_addr[device];
     return BT_OK;
@@ -125,6 +167,7 @@ extern "C" bt_status bt_bfc_noalloc(int device, const uint32_t *d_offsets, const
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
         return bt_fail(BT_ERR_NO_DEVICE, "gpu device id " + std::to_string(device) + " is not available");
+    DeviceGuard restore;  // the caller's current device comes back on every return
     BT_CUDA(cudaSetDevice(device));
     uint32_t *scratch = nullptr;
     BT_TRY(scratch_address(device, &scratch));

@@ -147,7 +147,8 @@ double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
  * [6] bucket splits; msp work: [8] peel tasks run, [9] neighbour slots
  * probed, [10] anchor slots, [11] butterflies found, [12] decrements, [13] m;
  * [14..16] nanoseconds the peeling kernel spent in level transitions, peel
- * phases and finalize phases; [20..27] SM cycles per CTA of the peeling
+ * phases and finalize phases; [17] bytes per working support of the last msp
+ * (4 when every support fits 32 bits, else 8); [20..27] SM cycles per CTA of the peeling
  * kernel by step: task lookup, anchor staging, slice load, probe pass, hit
  * pass, flushes, grid-barrier waits, other work.  After a batched call, [1] is
  * the sub-rounds summed over its arenas and [7] the number of arenas. */
@@ -283,9 +284,11 @@ bt_status bt_job_bytes(bt_ctx *ctx, const bt_graph *const *graphs, uint32_t coun
  * Scratch is one 32 MiB device array inside the library, held by every GPU
  * that loads it until the process exits; graphs with more than 4,194,304
  * vertices are rejected with BT_ERR_INVALID.  The first call on a device looks
- * up that array's device address (once per device) and should come before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race and give wrong counts. */
+ * up that array's device address (once per device and CUDA context: a call
+ * after cudaDeviceReset looks it up again) and should come before any stream
+ * capture.  The call restores the caller's current device before it returns.
+ * All calls share the array: calls that overlap on the GPU race and give
+ * wrong counts. */
 bt_status bt_bfc_noalloc(int device, const uint32_t *d_offsets, const uint32_t *d_neighbors,
                          uint32_t n, uint64_t m, unsigned long long *d_count, void *stream);
 

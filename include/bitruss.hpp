@@ -16,6 +16,8 @@
 // logged, and failures throw bt::Error instead of calling exit().
 #pragma once
 
+#include <atomic>
+#include <cstdint>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -34,26 +36,47 @@ inline void check(bt_status s, const char *what) {
         throw Error(s, std::string(what) + ": " + bt_status_string(s) + ": " + bt_last_error());
 }
 
-// One device context per host thread and device, created on first use.
+// Per host thread: one device context (created on first use, replaced when
+// another device is asked for) and the serial number of the Graph resident
+// on it (0: none).
+struct ThreadState {
+    bt_ctx *ctx = nullptr;
+    int dev = -1;
+    uint64_t resident = 0;
+    ThreadState() = default;
+    ThreadState(const ThreadState &) = delete;
+    ThreadState &operator=(const ThreadState &) = delete;
+    ~ThreadState() {
+        if (ctx) bt_ctx_free(ctx);
+    }
+};
+
+inline ThreadState &thread_state() {
+    static thread_local ThreadState s;
+    return s;
+}
+
 inline bt_ctx *thread_context(int device = -1) {
-    static thread_local bt_ctx *ctx = nullptr;
-    static thread_local int ctx_dev = -1;
-    static thread_local struct Reaper {
-        bt_ctx **p;
-        ~Reaper() {
-            if (*p) bt_ctx_free(*p);
-        }
-    } reaper{&ctx};
-    if (device >= 0 && ctx && ctx_dev != device) {
-        bt_ctx_free(ctx);
-        ctx = nullptr;
+    ThreadState &s = thread_state();
+    if (device >= 0 && s.ctx && s.dev != device) {
+        bt_ctx_free(s.ctx);
+        s.ctx = nullptr;
+        s.resident = 0;
     }
-    if (!ctx) {
+    if (!s.ctx) {
         int d = device >= 0 ? device : 0;
-        check(bt_ctx_create(d, &ctx), "bt_ctx_create");
-        ctx_dev = d;
+        s.resident = 0;
+        check(bt_ctx_create(d, &s.ctx), "bt_ctx_create");
+        s.dev = d;
     }
-    return ctx;
+    return s.ctx;
+}
+
+// Every Graph gets a serial number no other Graph of the process shares, so a
+// Graph built where a destroyed one lived is never mistaken for it.
+inline uint64_t next_graph_serial() {
+    static std::atomic<uint64_t> counter{0};
+    return ++counter;
 }
 
 class Graph {
@@ -74,7 +97,11 @@ public:
     }
     Graph(const Graph &) = delete;
     Graph &operator=(const Graph &) = delete;
-    ~Graph() { bt_graph_free(g_); }
+    ~Graph() {
+        ThreadState &s = thread_state();
+        if (s.resident == serial_) s.resident = 0;
+        bt_graph_free(g_);
+    }
 
     void graph_to_bin(const std::string &filename) const {
         check(bt_graph_save_bin(g_, filename.c_str()), "graph_to_bin");
@@ -94,15 +121,15 @@ public:
 
     const bt_graph *handle() const { return g_; }
 
-    // upload to the calling thread's context unless it already holds this graph
+    // upload to the calling thread's context unless it already holds this
+    // graph (keyed on the graph's serial number, not its address)
     bt_ctx *on_device(int device = -1) const {
         bt_ctx *ctx = thread_context(device);
-        static thread_local const void *resident = nullptr;
-        static thread_local bt_ctx *resident_ctx = nullptr;
-        if (resident != (const void *)this || resident_ctx != ctx) {
+        ThreadState &s = thread_state();
+        if (s.resident != serial_) {
+            s.resident = 0;  // a failed upload leaves no graph resident
             check(bt_graph_upload(ctx, g_), "graph upload");
-            resident = this;
-            resident_ctx = ctx;
+            s.resident = serial_;
         }
         return ctx;
     }
@@ -124,6 +151,7 @@ private:
         edge_ids = v.edge_ids;
     }
     bt_graph *g_ = nullptr;
+    const uint64_t serial_ = next_graph_serial();
 };
 
 // bfc_vpp(Graph*): src/bfc/bfc_vpp.cu:321-385

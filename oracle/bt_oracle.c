@@ -381,27 +381,30 @@ static inline void og_dec(og_peel *p, uint32_t e) {
  *          The corrected rule decrements the survivor iff uv is the smallest
  *          of the three frontier edges.  (exact == 1)
  */
-static inline void og_rule(og_peel *p, uint32_t uv, uint32_t wv, uint32_t wx, uint32_t ux,
-                           int exact) {
+static inline int og_rule(og_peel *p, uint32_t uv, uint32_t wv, uint32_t wx, uint32_t ux,
+                          int exact) {
     int pwv = !p->in_curr[wv], pwx = !p->in_curr[wx], pux = !p->in_curr[ux];
     int cnt = pwv + pwx + pux;
+    int d = 0;  /* unit decrements applied (returned for the byte count) */
     if (cnt == 3) {
         og_dec(p, wv); og_dec(p, wx); og_dec(p, ux);
+        d = 3;
     } else if (cnt == 2) {
-        if (pwv && pwx && uv < ux) { og_dec(p, wv); og_dec(p, wx); }
-        if (pwv && pux && uv < wx) { og_dec(p, wv); og_dec(p, ux); }
-        if (pwx && pux && uv < wv) { og_dec(p, wx); og_dec(p, ux); }
+        if (pwv && pwx && uv < ux) { og_dec(p, wv); og_dec(p, wx); d += 2; }
+        if (pwv && pux && uv < wx) { og_dec(p, wv); og_dec(p, ux); d += 2; }
+        if (pwx && pux && uv < wv) { og_dec(p, wx); og_dec(p, ux); d += 2; }
     } else if (cnt == 1) {
         if (!exact) {
-            if (pwx && uv < ux && ux < wv) og_dec(p, wx);
-            if (pwv && uv < ux && ux < wx) og_dec(p, wv);
-            if (pux && uv < wv && wv < wx) og_dec(p, ux);
+            if (pwx && uv < ux && ux < wv) { og_dec(p, wx); d++; }
+            if (pwv && uv < ux && ux < wx) { og_dec(p, wv); d++; }
+            if (pux && uv < wv && wv < wx) { og_dec(p, ux); d++; }
         } else {
-            if (pwx && uv < ux && uv < wv) og_dec(p, wx);
-            if (pwv && uv < ux && uv < wx) og_dec(p, wv);
-            if (pux && uv < wv && uv < wx) og_dec(p, ux);
+            if (pwx && uv < ux && uv < wv) { og_dec(p, wx); d++; }
+            if (pwv && uv < ux && uv < wx) { og_dec(p, wv); d++; }
+            if (pux && uv < wv && uv < wx) { og_dec(p, ux); d++; }
         }
     }
+    return d;
 }
 
 /* Peel one frontier edge by merging N(w) with N(u) for every w in N(v):
@@ -409,7 +412,7 @@ static inline void og_rule(og_peel *p, uint32_t uv, uint32_t wv, uint32_t wx, ui
  * (possibly compressed) rows. */
 static void og_peel_edge_merge(const og_graph *g, og_peel *p, const uint32_t *deg,
                                const uint32_t *nbr, const uint32_t *eid, uint32_t uv,
-                               int exact) {
+                               int exact, uint64_t *acc) {
     uint32_t u = g->edges[2 * (uint64_t)uv], v = g->edges[2 * (uint64_t)uv + 1];
     const uint32_t *un = nbr + g->offsets[u];
     uint32_t ul = deg[u];
@@ -427,7 +430,8 @@ static void og_peel_edge_merge(const og_graph *g, og_peel *p, const uint32_t *de
             uint32_t wx = eid[g->offsets[w] + j], ux = eid[g->offsets[u] + k];
             j++; k++;
             if (p->processed[ux] || p->processed[wx]) continue;
-            og_rule(p, uv, wv, wx, ux, exact);
+            acc[0]++;
+            acc[1] += (uint64_t)og_rule(p, uv, wv, wx, ux, exact);
         }
     }
 }
@@ -469,7 +473,7 @@ static inline int64_t og_find(const uint32_t *row, uint32_t d, uint32_t y) {
  */
 static void og_peel_edge_table(const og_graph *g, og_peel *p, const uint32_t *deg,
                                const uint32_t *nbr, const uint32_t *eid, const uint64_t *two_hop,
-                               uint32_t uv, int exact, uint32_t *pos) {
+                               uint32_t uv, int exact, uint32_t *pos, uint64_t *acc) {
     uint32_t u = g->edges[2 * (uint64_t)uv], v = g->edges[2 * (uint64_t)uv + 1];
     uint64_t cost_v = two_hop[v], cost_u = two_hop[u];
     /* walk: iterate mid in N(piv)\anchor, probe N(mid) against N(anchor) */
@@ -507,9 +511,10 @@ static void og_peel_edge_table(const og_graph *g, og_peel *p, const uint32_t *de
             uint32_t e_my = eid[g->offsets[mid] + (uint64_t)jm];
             uint32_t e_ay = eid[g->offsets[anc] + (uint64_t)ka];
             if (p->processed[e_ay] || p->processed[e_my]) continue;
+            acc[0]++;
             /* name the edges as the reference does: w on u's side, x on v's */
-            if (piv == v) og_rule(p, uv, e_pm, e_my, e_ay, exact); /* mid=w, y=x */
-            else og_rule(p, uv, e_ay, e_my, e_pm, exact);          /* mid=x, y=w */
+            if (piv == v) acc[1] += (uint64_t)og_rule(p, uv, e_pm, e_my, e_ay, exact); /* mid=w, y=x */
+            else acc[1] += (uint64_t)og_rule(p, uv, e_ay, e_my, e_pm, exact);          /* mid=x, y=w */
         }
     }
     if (table)
@@ -546,7 +551,18 @@ static uint64_t og_compress(const og_graph *g, const uint64_t *sup, uint64_t lev
  * Compression follows the reference trigger (edge_num <= live/2 and
  * live >= m/10) and re-filters the current rows each time.
  * Returns the reference's "levels" figure (last level that peeled edges).
- * stats (optional, 4 entries): levels, sub-rounds, compressions, peeled edges.
+ * stats (optional, 8 entries): levels, sub-rounds, compressions, peeled edges,
+ * then the algorithmic bytes of the peeling in the reference's own walk
+ * (bitruss_msp.cu:187-274: for a frontier edge uv, u = its U end and v = its
+ * V end, u's row is staged once, v's row is read with edge ids, and every
+ * live w in N(v) minus u has its row merged with u's), with d_s(x) = the
+ * number of x's edges unprocessed when sub-round s starts:
+ *   [4] row bytes  = sum over sub-rounds s and uv in the frontier of s of
+ *                    4 d_s(u) + 8 d_s(v) + sum_{live w in N(v), w != u} 4 d_s(w)
+ *   [5] butterflies visited (all four edges unprocessed at the start of s)
+ *   [6] unit decrements the rule applied
+ *   [7] total = [4] + 8 [5] (two edge ids per butterfly) + 8 [6] (a support
+ *       read-modify-write per decrement).
  * max_seconds > 0 bounds the run for timing samples: it stops after the first
  * sub-round that ends past the deadline (the result is then partial).
  */
@@ -575,10 +591,20 @@ uint64_t og_msp(const og_graph *g, int threads, uint64_t *sup, int mode, uint64_
     uint32_t *alive = malloc(sizeof(uint32_t) * (m ? m : 1));
     uint64_t alive_len = 0;
     int64_t edge_num = (int64_t)m;
+    /* live degrees for the byte count: ldeg[x] = x's unprocessed edges */
+    uint32_t *ldeg = malloc(sizeof(uint32_t) * (g->n ? g->n : 1));
+    memcpy(ldeg, g->degrees, sizeof(uint32_t) * g->n);
     for (uint64_t e = 0; e < m; e++) {
-        if (sup[e] == 0) { p.processed[e] = 1; edge_num--; }
-        else alive[alive_len++] = (uint32_t)e;
+        if (sup[e] == 0) {
+            p.processed[e] = 1;
+            edge_num--;
+            ldeg[g->edges[2 * e]]--;
+            ldeg[g->edges[2 * e + 1]]--;
+        } else {
+            alive[alive_len++] = (uint32_t)e;
+        }
     }
+    uint64_t row_bytes = 0, visited = 0, decs = 0;
 
     /* Table mode finds each level's frontier without scanning every live
      * edge (the reference scans all m edges per level, which is what makes a
@@ -673,18 +699,36 @@ uint64_t og_msp(const og_graph *g, int threads, uint64_t *sup, int mode, uint64_
                         (unsigned long long)subrounds, (unsigned long long)level,
                         (long long)edge_num, omp_get_wtime() - t_start);
             p.next_len = 0;
-#pragma omp parallel
+            uint64_t sr_bytes = 0, sr_visited = 0, sr_decs = 0;
+#pragma omp parallel reduction(+ : sr_bytes, sr_visited, sr_decs)
             {
                 uint32_t *pos = table ? pos_of[omp_get_thread_num()] : NULL;
 #pragma omp for schedule(dynamic, 1)
                 for (uint64_t i = 0; i < curr_len; i++) {
-                    if (table) og_peel_edge_table(g, &p, deg, nbr, eid, two_hop, curr[i], exact, pos);
-                    else og_peel_edge_merge(g, &p, deg, nbr, eid, curr[i], exact);
+                    const uint32_t uv = curr[i];
+                    /* the reference walk's row bytes for uv (see above) */
+                    const uint32_t u = g->edges[2 * (uint64_t)uv], v = g->edges[2 * (uint64_t)uv + 1];
+                    uint64_t b = 4ull * ldeg[u] + 8ull * ldeg[v];
+                    for (uint32_t x = 0; x < deg[v]; x++) {
+                        const uint32_t w = nbr[g->offsets[v] + x];
+                        if (w != u && !p.processed[eid[g->offsets[v] + x]]) b += 4ull * ldeg[w];
+                    }
+                    sr_bytes += b;
+                    uint64_t acc[2] = {0, 0};
+                    if (table) og_peel_edge_table(g, &p, deg, nbr, eid, two_hop, uv, exact, pos, acc);
+                    else og_peel_edge_merge(g, &p, deg, nbr, eid, uv, exact, acc);
+                    sr_visited += acc[0];
+                    sr_decs += acc[1];
                 }
             }
+            row_bytes += sr_bytes;
+            visited += sr_visited;
+            decs += sr_decs;
             for (uint64_t i = 0; i < curr_len; i++) {
                 p.processed[curr[i]] = 1;
                 p.in_curr[curr[i]] = 0;
+                ldeg[g->edges[2 * (uint64_t)curr[i]]]--;
+                ldeg[g->edges[2 * (uint64_t)curr[i] + 1]]--;
             }
             /* swap(curr, next), swap(is_in_curr, is_in_next) */
             memcpy(curr, p.next, sizeof(uint32_t) * p.next_len);
@@ -721,7 +765,12 @@ uint64_t og_msp(const og_graph *g, int threads, uint64_t *sup, int mode, uint64_
         stats[1] = subrounds;
         stats[2] = compressions;
         stats[3] = peeled;
+        stats[4] = row_bytes;
+        stats[5] = visited;
+        stats[6] = decs;
+        stats[7] = row_bytes + 8 * visited + 8 * decs;
     }
+    free(ldeg);
     free(p.processed); free(p.in_curr); free(p.in_next); free(p.next);
     free(curr); free(deg); free(nbr); free(eid);
     return last;

@@ -24,7 +24,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref.so")
-REF_SRC = "/root/reference/src"
+# Root of the reference's source tree (read-only); only the recipes that
+# compile or read the reference use it.
+REF_ROOT = os.environ.get("BITRUSS_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 
 _u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
 _u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
@@ -44,7 +47,7 @@ def build(ref: bool | None = None) -> None:
     are present, or when ``ref`` is True)."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     if ref or (ref is None and os.path.isdir(REF_SRC)):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
 
 
 _lib = None
@@ -155,14 +158,17 @@ MSP_REF, MSP_EXACT, MSP_TABLE, MSP_TABLE_EXACT = 0, 1, 2, 3
 def msp(g: dict, threads: int = 0, mode: int = MSP_REF, sup=None, max_seconds: float = 0.0):
     """(uint64 bitruss[m], levels, stats) -- cpu_bitruss.cpp:563-624.
 
-    stats = [levels, sub-rounds, compressions, peeled edges].  max_seconds > 0
+    stats = [levels, sub-rounds, compressions, peeled edges, row bytes,
+    butterflies visited, unit decrements, algorithmic bytes]: the last four
+    are the byte count of the reference's own peeling walk
+    (bitruss_msp.cu:187-274; see og_msp in bt_oracle.c).  max_seconds > 0
     stops early (partial result, for bounded timing samples)."""
     if sup is None:
         sup, _ = ebfc(g, threads)
     work = np.array(sup, dtype=np.uint64, copy=True)
     if work.size == 0:
         work = np.zeros(1, np.uint64)
-    stats = np.zeros(4, np.uint64)
+    stats = np.zeros(8, np.uint64)
     s = _gs(g)
     levels = lib().og_msp(C.byref(s), threads, work, mode, stats, max_seconds)
     return work[: g["m"]], int(levels), [int(x) for x in stats]

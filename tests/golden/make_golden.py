@@ -39,7 +39,7 @@ sys.path.insert(0, ROOT)
 from gpu_bitruss_gb300 import gen  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-AW = "/root/reference/data/aw.graph"
+AW = os.path.join(O.REF_ROOT, "data", "aw.graph")  # the reference's sample graph
 
 
 def cases():

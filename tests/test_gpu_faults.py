@@ -1,5 +1,6 @@
 """Failure handling on the GPU, without faulting it: a device-side wait that
-runs out, an allocation refused by the memory budget, and the coh front end.
+runs out, an allocation refused by the memory budget, the coh front end and
+the C++ drop-in header.
 
 The waits in the peeling kernel (its grid barrier) are bounded.  With a 1 us
 limit some CTA is sure to wait longer for the others; the kernel must then
@@ -12,7 +13,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import ROOT, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -91,3 +92,31 @@ def test_coh_gpu_msp_end_to_end(engine, tmp_path):
         [engine.COH_PATH, "--graph", str(binf), "--gpu", "--algo", "msp"], capture_output=True, text=True).stdout
     r = subprocess.run([engine.COH_PATH, "--graph", str(binf), "--gpu", "--algo", "bfc"], capture_output=True, text=True)
     assert f"btf number: {int(gd['bfc'])}" in r.stdout
+
+
+def test_cpp_header_graph_loop_uploads_every_graph(engine, tmp_path):
+    """bitruss.hpp in a loop over files, one stack Graph per iteration (the
+    same address each time): each file's results equal its own goldens."""
+    src = os.path.join(ROOT, "tests", "cpp", "hpp_graph_loop.cpp")
+    exe = tmp_path / "hpp_graph_loop"
+    pkg = os.path.dirname(engine.LIB_PATH)
+    r = subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", str(exe),
+                        "-L", pkg, "-lbitruss", f"-Wl,-rpath,{pkg}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    names = ["aw", "er_config1", "er_small0", "aw", "er_config1"]
+    files = []
+    for i, name in enumerate(names):
+        gd = load_golden(name)
+        p = tmp_path / f"g{i}.txt"
+        p.write_text("".join(f"{a} {b}\n" for a, b in zip(gd["u"].tolist(), gd["v"].tolist())))
+        files.append(str(p))
+    r = subprocess.run([str(exe)] + files, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert len(lines) == len(names)
+    for name, line in zip(names, lines):
+        gd = load_golden(name)
+        vals = np.array(line.split(), dtype=np.uint64)
+        assert vals[0] == gd["bfc"], name
+        assert vals[1] == gd["levels"], name
+        np.testing.assert_array_equal(vals[2:], gd["msp"], err_msg=name)

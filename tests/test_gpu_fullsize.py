@@ -1,5 +1,5 @@
 """Config 2 at full size (Chung-Lu, 20M edges), against facts the oracle
-computed (tests/golden/make_cl20m.py): butterfly count, largest support and
+computed (tests/golden/make_facts.py): butterfly count, largest support and
 the digest of all 20M supports, bit for bit; size-independent properties of
 the decomposition; and -- when the oracle's full decomposition is recorded in
 tests/golden/cl20m.json -- the digest of the msp result itself."""
