@@ -255,6 +255,8 @@ def run_ours(args):
     ctx = bt.Context(local)
     stream = torch.cuda.Stream(device=local)
     ctx.set_stream(stream.cuda_stream)
+    if args.schedule:
+        ctx.set_msp_schedule(*[int(x) for x in args.schedule.split(",")])
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
     out = np.zeros(max(m, 1), np.uint32)
     # H2D per step: offsets, degrees, neighbours and edge ids of the host CSR
@@ -337,6 +339,7 @@ def run_ours(args):
                    "levels": stats[0], "subrounds": stats[1], "tasks": stats[3],
                    "peel_ms": statistics.median(peels), "step_device_ms": statistics.median(devs),
                    "step_wall_ms": statistics.median(walls), "gen_s": round(t_gen, 1),
+                   "schedule": list(ctx.msp_schedule()),
                    "kernel_phase_ms": {"level_transitions": work[6] / 1e6, "peel": work[7] / 1e6},
                    "cta_ms_by_step": dict(zip(["task", "stage", "slice", "probe", "hits", "flush",
                                                "barrier", "other"],
@@ -613,6 +616,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of CPU peeling per sample step")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--schedule", default="",
+                    help="msp task schedule 'min_grain,tasks_per_cta,local_plan' (default: built-in)")
     ap.add_argument("--rates", default="100,1000,5000", help="serve: request rates (req/s)")
     ap.add_argument("--requests", type=int, default=200, help="serve: requests per rate")
     ap.add_argument("--pool", type=int, default=96, help="serve: graphs of the batch distribution")

@@ -282,9 +282,9 @@ extern "C" bt_status bt_ctx_set_msp_schedule(bt_ctx *ctx, uint32_t min_grain, ui
 
 extern "C" bt_status bt_ctx_get_msp_schedule(const bt_ctx *ctx, uint32_t *out) {
     if (!ctx || !out) return bt_fail(BT_ERR_INVALID, "null argument");
-    out[0] = ctx->msp_schedule[0] ? ctx->msp_schedule[0] : 2048;
-    out[1] = ctx->msp_schedule[1] ? ctx->msp_schedule[1] : 2;
-    out[2] = ctx->msp_schedule[2] ? ctx->msp_schedule[2] : 512;
+    out[0] = ctx->msp_schedule[0] ? ctx->msp_schedule[0] : kMspMinGrain;
+    out[1] = ctx->msp_schedule[1] ? ctx->msp_schedule[1] : kMspTasksPerCta;
+    out[2] = ctx->msp_schedule[2] ? ctx->msp_schedule[2] : kMspLocalPlan;
     return BT_OK;
 }
 
@@ -295,7 +295,7 @@ extern "C" bt_status bt_msp_autotune(bt_ctx *ctx, uint32_t *out, double *best_ms
     BT_TRY(enter_ctx(ctx));
     if (!ctx->has_graph) return bt_fail(BT_ERR_STATE, "no graph uploaded to this context");
     static const uint32_t grains[] = {512, 1024, 2048, 4096, 8192};
-    static const uint32_t tasks[] = {1, 2, 3, 4};
+    static const uint32_t tasks[] = {1, 2, 4, 8};
     static const uint32_t plans[] = {64, 256, 512};
     uint32_t cur[3];
     BT_TRY(bt_ctx_get_msp_schedule(ctx, cur));

@@ -33,11 +33,23 @@
 // in N[z]; edge (u, v) with value h is recomputed iff lo < h <= hi at u or at
 // v.  The test never skips an edge that could change, so values, and the
 // number of rounds, are those of the full synchronous iteration.
+//
+// Starting values.  The reference starts from the butterfly supports.  The
+// iteration is monotone: started from any values s with b <= s <= supports,
+// where b are the bitruss numbers (the largest fixpoint below the supports),
+// every round keeps the values at or above b and they converge to the
+// largest fixpoint below s, which is b.  So the result does not depend on
+// the start, only the number of rounds does.  Graphs of up to 2^20 edges
+// start from the supports (the reference's rounds); larger graphs start from
+// the exact peel's values (bt_msp_exact, the bitruss numbers themselves),
+// and the rounds then verify that those values are the fixpoint: one round
+// that changes nothing.  BT_HIDX_START=support or =peel picks the start.
 #include <cub/device/device_select.cuh>
 #include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "bt_device.cuh"
 #include "bt_internal.h"
@@ -300,6 +312,13 @@ __global__ void k_hidx_flags(uint64_t m, const unsigned long long *val, const ui
     }
 }
 
+// starting values from a uint32 result (the exact peel)
+__global__ void k_hidx_widen(uint64_t m, const uint32_t *in, unsigned long long *v) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+         e += (uint64_t)gridDim.x * blockDim.x)
+        v[e] = in[e];
+}
+
 __global__ void k_hidx_result(uint64_t m, const unsigned long long *v, uint32_t *out, unsigned *overflow) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
          e += (uint64_t)gridDim.x * blockDim.x) {
@@ -310,9 +329,23 @@ __global__ void k_hidx_result(uint64_t m, const unsigned long long *v, uint32_t 
 
 }  // namespace
 
+// Start of the iteration: true = the exact peel's values, false = supports.
+static bool hidx_from_peel(uint64_t m) {
+    const char *v = getenv("BT_HIDX_START");
+    if (v && !strcmp(v, "peel")) return true;
+    if (v && !strcmp(v, "support")) return false;
+    return m > (1ull << 20);
+}
+
 bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
-    uint64_t dummy = 0;
-    BT_TRY(dev_ebfc(ctx, true, &dummy));
+    const bool from_peel = hidx_from_peel(ctx->g.m);
+    if (from_peel) {
+        uint32_t lv = 0;
+        BT_TRY(dev_msp(ctx, true, &lv));  // ctx->result = the exact peel's values
+    } else {
+        uint64_t dummy = 0;
+        BT_TRY(dev_ebfc(ctx, true, &dummy));
+    }
     DevGraph &g = ctx->g;
     cudaStream_t st = ctx->stream;
     const uint64_t m = g.m, n = g.n;
@@ -361,11 +394,16 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     // count, [4] active count
     uint32_t *marked_len = (uint32_t *)(ctr + 3);
     unsigned long long *active_len = ctr + 4;
-    C(cudaMemcpyAsync(val, ctx->sup, 8 * m, cudaMemcpyDeviceToDevice, st));
     C(cudaMemsetAsync(mark, 0, 4 * nn, st));
     bt::Rows rows{g.off, g.deg0, g.nbr0, g.eid0, g.hub_base, g.hub_mask, g.hub_pool};
     const unsigned blk = 256, cap = (unsigned)ctx->sm_count * 8;
     const unsigned egrid = (unsigned)std::min<uint64_t>((mm + blk - 1) / blk, cap);
+    if (!from_peel) {
+        C(cudaMemcpyAsync(val, ctx->sup, 8 * m, cudaMemcpyDeviceToDevice, st));
+    } else if (m) {
+        k_hidx_widen<<<egrid, blk, 0, st>>>(m, ctx->result, val); bt_note_launches(1);
+        C(cudaGetLastError());
+    }
     if (n) {
         k_row_prefix<<<(unsigned)std::min<uint64_t>((n * 32 + blk - 1) / blk, cap), blk, 0, st>>>(
             rows, g.n, rowpre, two_hop); bt_note_launches(1);
@@ -439,7 +477,8 @@ bt_status dev_hidx(bt_ctx *ctx, uint32_t *rounds) {
     release();
     if (overflow) return bt_fail(BT_ERR_OVERFLOW, "hidx: a bitruss number exceeds uint32");
     ctx->stats[4] = r;
-    ctx->work[9] = recomputed;  // edge recomputations over all rounds
+    ctx->work[10] = recomputed;  // edge recomputations over all rounds
+    ctx->work[11] = from_peel ? 1 : 0;
     ctx->last_result = 2;
     if (rounds) *rounds = r;
     return BT_OK;

@@ -135,6 +135,12 @@ struct bt_ctx {
     uint64_t arena_edges = 1ull << 28;  // batched calls: edges per arena, at most
 };
 
+// Default msp task schedule (bt_ctx_set_msp_schedule with 0 picks these):
+// probe positions per task at least, tasks per CTA, local-plan limit.
+constexpr uint32_t kMspMinGrain = 2048;
+constexpr uint32_t kMspTasksPerCta = 2;
+constexpr uint32_t kMspLocalPlan = 512;
+
 enum { PH_UPLOAD = 0, PH_EBFC = 1, PH_PEEL = 2, PH_HIDX = 3, PH_TOTAL = 4, PH_MSP = 5 };
 
 // device arena (tracked against the context's budget)

@@ -40,8 +40,10 @@
 //    from the shorter side, hits queued in shared memory and ruled on in a
 //    dense pass; decrements of the pivot-side and anchor-side edges are summed
 //    in shared memory and flushed once.
-//  * Processed edges are dropped from the rows (device-side compaction) with
-//    the reference's trigger (:537-549), which only changes work, not results.
+//  * Processed edges are dropped from the rows (device-side compaction)
+//    whenever the live edges have halved (the reference's trigger, :537-549,
+//    without its floor at a tenth of the edges); compaction only changes
+//    work, not results.
 // Grid barriers are bounded by a time limit; an expired wait sets an error and
 // the kernel returns.
 #include <cstdio>
@@ -56,9 +58,7 @@ namespace {
 
 using bt::kEmpty;
 using bt::kThreads;
-constexpr uint32_t kMinGrain = 2048;    // default: plain probe positions per task, at least
-constexpr uint32_t kTasksPerCta = 2;    // default: tasks per CTA a sub-round's work is cut into
-constexpr uint32_t kLocalPlan = 512;    // frontiers up to this size may be planned by every CTA
+constexpr uint32_t kLocalPlan = kMspLocalPlan;  // largest frontier every CTA may plan itself
 
 struct MspState {
     bt::Barrier bar;
@@ -98,6 +98,10 @@ struct MspArgs {
     MspState *s;
     uint32_t n, nblocks, exact;
     uint32_t min_grain, tasks_per_cta, local_plan;  // task schedule (results do not depend on it)
+    // row compaction trigger: compact when the live edges fall to cfrac of
+    // the live edges at the last compaction, while those were at least
+    // cfloor * m (compaction changes work, never results)
+    float cfrac, cfloor;
     uint64_t m;
     unsigned long long wait_ns;
     const uint32_t *off;
@@ -597,9 +601,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_msp(MspArgs a) {
                     a.near_b[atomicAdd(&s->near_ctr[nsel ^ 1], 1u)] = e;
                 }
             }
-            // T4: compression (reference trigger, bitruss_msp.cu:537)
-            const bool squeeze = (double)s->edge_num <= 0.5 * (double)s->live_at_compress &&
-                                 (double)s->live_at_compress >= 0.1 * (double)a.m;
+            // T4: compression (the reference's trigger, bitruss_msp.cu:537, see cfrac)
+            const bool squeeze = (double)s->edge_num <= (double)a.cfrac * (double)s->live_at_compress &&
+                                 (double)s->live_at_compress >= (double)a.cfloor * (double)a.m;
             if (!barrier(a, sm)) return;
             {
                 uint32_t *t = a.near_a; a.near_a = a.near_b; a.near_b = t;
@@ -816,10 +820,26 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     a.n = g.n;
     a.m = m;
     a.exact = exact ? 1u : 0u;
-    a.min_grain = ctx->msp_schedule[0] ? ctx->msp_schedule[0] : kMinGrain;
-    a.tasks_per_cta = ctx->msp_schedule[1] ? ctx->msp_schedule[1] : kTasksPerCta;
+    a.min_grain = ctx->msp_schedule[0] ? ctx->msp_schedule[0] : kMspMinGrain;
+    a.tasks_per_cta = ctx->msp_schedule[1] ? ctx->msp_schedule[1] : kMspTasksPerCta;
     a.local_plan = ctx->msp_schedule[2] ? std::min(ctx->msp_schedule[2], kLocalPlan) : kLocalPlan;
     a.wait_ns = wait_limit_ns();
+    // Row compaction: whenever the live edges have halved since the last
+    // compaction.  The reference also stops compacting once fewer than a tenth
+    // of all edges are live (bitruss_msp.cu:537), which leaves the long tail
+    // of the peel walking rows full of processed edges; dropping that floor
+    // cut the row positions walked on the 20M-edge Chung-Lu graph by 11%.
+    // Compaction changes which rows are walked, never a result.
+    // BT_MSP_COMPACT="frac,floor" sets the trigger (the reference's is 0.5,0.1).
+    a.cfrac = 0.5f;
+    a.cfloor = 0.0f;
+    if (const char *cv = getenv("BT_MSP_COMPACT")) {
+        float f = 0, fl = 0;
+        if (sscanf(cv, "%f,%f", &f, &fl) == 2 && f > 0 && f < 1 && fl >= 0 && fl <= 1) {
+            a.cfrac = f;
+            a.cfloor = fl;
+        }
+    }
     a.off = g.off;
     a.ends = g.ends;
     a.hub_base = g.hub_base;

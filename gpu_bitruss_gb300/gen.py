@@ -179,13 +179,21 @@ def batch_graph(i: int, count: int = 4096, sizes=None):
 
 def by_name(name: str):
     """Named workloads: aw (the reference's fixture), er, cl20m, hub100m,
-    and scaled-down Chung-Lu cases cl<k>k (k thousand edges) for tests."""
+    scaled-down Chung-Lu cases cl<k>k and scaled-down hub-skewed cases
+    hub<k>k (k thousand edges) for tests."""
     if name == "er":
         return er()
     if name == "cl20m":
         return chung_lu()
     if name == "hub100m":
         return hub_skew()
+    if name.startswith("hub") and name.endswith("k") and name[3:-1].isdigit():
+        # the hub100m shape scaled to k thousand edges: |U|, |V| and the hub
+        # cap scale with m, the mean V degree (20) stays
+        k = int(name[3:-1]) * 1000
+        scale = k / 100_000_000
+        return hub_skew(max(int(100_000 * scale), 16), max(int(5_000_000 * scale), 16), k,
+                        1.8, max(1_000_000 * scale, 16.0), seed=3)
     if name.startswith("cl") and name.endswith("k") and name[2:-1].isdigit():
         k = int(name[2:-1]) * 1000
         # same shape as cl20m, vertex counts scaled with m

@@ -120,7 +120,12 @@ bt_status bt_ebfc(bt_ctx *ctx, uint64_t *sup, uint64_t *count, uint64_t *support
 
 /* h-index bitruss numbers (true bitruss).  Replaces g_bitruss_hindex(Graph*):
  * bitruss_hidx.cu:179-256.  bitruss: m entries (NULL: device only);
- * rounds may be NULL. */
+ * rounds may be NULL.  The iteration's fixpoint does not depend on where it
+ * starts between the bitruss numbers and the supports: graphs of up to 2^20
+ * edges start from the supports, as the reference does (same rounds); larger
+ * graphs start from the exact peel's values (bt_msp_exact), and `rounds`
+ * counts the rounds that verify them (1 when they are the fixpoint).  The
+ * environment variable BT_HIDX_START=support|peel picks the start. */
 bt_status bt_hidx(bt_ctx *ctx, uint32_t *bitruss, uint32_t *rounds);
 
 /* Multi-stage peeling (GBiD).  Replaces bitruss_msp(Graph*):
@@ -148,7 +153,9 @@ double bt_ctx_phase_ms(const bt_ctx *ctx, const char *phase);
  * probed, [10] anchor slots, [11] butterflies found, [12] decrements, [13] m;
  * [14..16] nanoseconds the peeling kernel spent in level transitions, peel
  * phases and finalize phases; [17] bytes per working support of the last msp
- * (4 when every support fits 32 bits, else 8); [20..27] SM cycles per CTA of the peeling
+ * (4 when every support fits 32 bits, else 8); [18] edge recomputations of
+ * the last hidx over all its rounds, [19] 1 if it started from the exact
+ * peel's values, 0 if from the supports; [20..27] SM cycles per CTA of the peeling
  * kernel by step: task lookup, anchor staging, slice load, probe pass, hit
  * pass, flushes, grid-barrier waits, other work.  After a batched call, [1] is
  * the sub-rounds summed over its arenas and [7] the number of arenas. */

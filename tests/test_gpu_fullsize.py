@@ -39,3 +39,63 @@ def test_cl20m_counts_and_decomposition(engine, gpu_ctx):
         assert levels == want["levels"]
     if "subrounds" in want:
         assert gpu_ctx.stats()[1] == want["subrounds"]
+
+
+def test_hub100m_counts(engine):
+    """Config 3 at full size (hub-skewed, 100M edges, hubs of ~10^6
+    neighbours): butterfly count, largest support and the digest of all 100M
+    supports against the oracle's (tests/golden/hub100m.json)."""
+    from gpu_bitruss_gb300 import gen
+    with open(os.path.join(GOLDEN, "hub100m.json")) as f:
+        want = json.load(f)
+    u, v = gen.by_name("hub100m")
+    assert gen.digest(u, v) == want["edge_digest"]
+    g = engine.Graph.from_edges(u, v)
+    del u, v
+    assert g.m == want["m"]
+    ctx = engine.Context(0)
+    try:
+        ctx.upload(g)
+        assert ctx.bfc() == want["count"]
+        sup, count, sup_max = ctx.ebfc()
+        assert count == want["count"] and sup_max == want["support_max"]
+        assert hashlib.sha256(sup.astype("<u8").tobytes()).hexdigest() == want["sup_sha256"]
+    finally:
+        ctx.close()
+        g.close()
+
+
+@pytest.mark.parametrize("name", ["hub500k", "hub2000k"])
+def test_hub_family_vs_oracle(engine, gpu_ctx, name, monkeypatch):
+    """The config-3 shape (power-law U side with hubs, near-uniform V side)
+    scaled to what the CPU oracle decomposes: supports, msp (the reference
+    rule) with its level and sub-round counts, and exact msp, against the
+    oracle's digests (tests/golden/<name>.json); the msp result must not
+    change with 64-bit working supports or with another task schedule."""
+    from gpu_bitruss_gb300 import gen
+    path = os.path.join(GOLDEN, f"{name}.json")
+    if not os.path.exists(path):
+        pytest.skip(f"no oracle facts for {name}")
+    with open(path) as f:
+        want = json.load(f)
+    u, v = gen.by_name(name)
+    assert gen.digest(u, v) == want["edge_digest"]
+    g = engine.Graph.from_edges(u, v)
+    gpu_ctx.upload(g)
+    sup, count, sup_max = gpu_ctx.ebfc()
+    assert count == want["count"] and sup_max == want["support_max"]
+    assert hashlib.sha256(sup.astype("<u8").tobytes()).hexdigest() == want["sup_sha256"]
+    digest = lambda b: hashlib.sha256(b.astype("<u4").tobytes()).hexdigest()  # noqa: E731
+    b, levels = gpu_ctx.msp()
+    assert digest(b) == want["msp_sha256"]
+    assert levels == want["levels"] and gpu_ctx.stats()[1] == want["subrounds"]
+    x, _ = gpu_ctx.msp(exact=True)
+    assert digest(x) == want["exact_sha256"]
+    monkeypatch.setenv("BT_MSP_WIDE", "1")
+    assert digest(gpu_ctx.msp()[0]) == want["msp_sha256"]
+    monkeypatch.delenv("BT_MSP_WIDE")
+    gpu_ctx.set_msp_schedule(1024, 8, 64)
+    try:
+        assert digest(gpu_ctx.msp()[0]) == want["msp_sha256"]
+    finally:
+        gpu_ctx.set_msp_schedule(0, 0, 0)

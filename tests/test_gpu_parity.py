@@ -141,8 +141,30 @@ def test_hidx_rounds_match_the_oracle(engine, gpu_ctx, oracle_mod, name):
     np.testing.assert_array_equal(h.astype(np.uint64), gd["hidx"])
     want, want_rounds = oracle_mod.hidx(oracle_mod.build_csr(gd["u"], gd["v"]), 1)
     assert rounds == want_rounds
-    recomputed = gpu_ctx.stats()[17]
+    st = gpu_ctx.stats()
+    recomputed = st[18]
     assert g.m <= recomputed <= rounds * g.m
+    assert st[19] == 0  # started from the supports, as the reference does
+
+
+@pytest.mark.parametrize("name", ["aw", "er_config1", "er_small2", "er_small3", "cl5k", "cl20k", "sparse"])
+def test_hidx_from_the_exact_peel_reaches_the_same_fixpoint(engine, gpu_ctx, name, monkeypatch):
+    """Started from the exact peel's values instead of the supports, the
+    h-index iteration ends at the same per-edge values (the reference's
+    hidx), after one round that changes nothing."""
+    gd = load_golden(name)
+    g = engine.Graph.from_edges(gd["u"], gd["v"])
+    gpu_ctx.upload(g)
+    monkeypatch.setenv("BT_HIDX_START", "peel")
+    h, rounds = gpu_ctx.hidx()
+    np.testing.assert_array_equal(h.astype(np.uint64), gd["hidx"])
+    st = gpu_ctx.stats()
+    assert rounds == 1 and st[19] == 1
+    assert st[18] == g.m
+    monkeypatch.setenv("BT_HIDX_START", "support")
+    h2, rounds2 = gpu_ctx.hidx()
+    np.testing.assert_array_equal(h2, h)
+    assert gpu_ctx.stats()[19] == 0 and rounds2 >= 1
 
 
 @pytest.mark.parametrize("name", ["aw", "er_config1", "er_small3", "cl5k", "cl20k"])
