@@ -211,3 +211,23 @@ def test_schedule_arguments_are_checked(engine):
     assert L.bt_ctx_set_msp_schedule(None, 0, 0, 0) == 1
     assert L.bt_ctx_set_arena_edges(None, 10) == 1
     assert L.bt_msp_batch(None, None, 0, 0, None, None) == 1
+
+
+@pytest.mark.gpu
+def test_msp_batch_on_the_batch_distribution_vs_oracle(engine, gpu_ctx, oracle_mod):
+    """Graphs of the 4,096-graph batch itself (m log-uniform in [1e3, 2e6],
+    Chung-Lu gamma 2.3, seed 4+i): the first ten of them small enough for the
+    CPU oracle, packed in one arena; every graph's bitruss numbers and level
+    count equal the oracle's."""
+    from gpu_bitruss_gb300 import gen
+    O = oracle_mod
+    sizes = gen.batch_sizes()
+    picks = [i for i in range(200) if sizes[0][i] <= 150_000][:10]
+    lists = [gen.batch_graph(i, sizes=sizes) for i in picks]
+    graphs = [engine.Graph.from_edges(u, v) for u, v in lists]
+    res, levels = gpu_ctx.msp_batch(graphs)
+    for (u, v), r, lv in zip(lists, res, levels):
+        g = O.build_csr(u, v)
+        want, wl, _ = O.msp(g, 0, O.MSP_TABLE)
+        np.testing.assert_array_equal(r.astype(np.uint64), want)
+        assert int(lv) == wl
