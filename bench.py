@@ -96,13 +96,16 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes per k_msp launch, measured by ncu on graphs larger than L2 but
+# small enough to capture (profiles/k_msp_dram_traffic.md).  The traffic per
+# row position grows with the graph (2M edges: 1.27 B, 5M: 10.85 B), so it is
+# not scaled to other sizes: other workloads report none.
+DRAM_TRAFFIC = {"cl2000k": 16_232_689_408 + 2_250_057_728, "cl5000k": 624_777_743_872 + 71_806_630_400}
+
+
 def load_traffic(workload):
-    """DRAM bytes per k_msp launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "k_msp_traffic.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return d.get(workload)
-    return None
+    """DRAM bytes of one k_msp launch on this workload, where measured."""
+    return DRAM_TRAFFIC.get(workload)
 
 
 class ClockSampler:
@@ -350,6 +353,9 @@ def run_ours(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_note": "ncu DRAM bytes per launch exist for cl2000k and cl5000k only "
+                                     "(profiles/k_msp_dram_traffic.md); they do not scale in "
+                                     "proportion to the work, so none is given for other graphs",
                      "peak_source": f"{peak_kind} hbm_gbs", "kernel": "k_msp",
                      "algorithmic_bytes": int(alg_bytes), "algorithmic_bytes_source": alg_src,
                      "kernel_counted": {"bytes": int(kernel_bytes),

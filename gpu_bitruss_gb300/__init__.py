@@ -50,7 +50,7 @@ SYMBOLS = [
     "bt_ctx_phase_ms", "bt_ctx_stats", "bt_status_string", "bt_last_error",
     "bt_bfc_noalloc",
     "bt_ctx_set_msp_schedule", "bt_ctx_get_msp_schedule", "bt_msp_autotune",
-    "bt_graph_pack", "bt_ctx_set_arena_edges", "bt_msp_batch", "bt_ebfc_batch",
+    "bt_graph_pack", "bt_ctx_set_arena_edges", "bt_ctx_set_peel_ctas", "bt_msp_batch", "bt_ebfc_batch",
     "bt_ctx_memory_peak", "bt_server_create", "bt_server_submit", "bt_server_wait",
     "bt_server_latency", "bt_server_stats", "bt_server_free", "bt_job_bytes",
     "bt_kernel_launches",
@@ -130,6 +130,7 @@ def load():
         "bt_msp_autotune": ([P, P, C.POINTER(C.c_double)], i32),
         "bt_graph_pack": ([P, u32, C.POINTER(P), P], i32),
         "bt_ctx_set_arena_edges": ([P, u64], i32),
+        "bt_ctx_set_peel_ctas": ([P, u32], i32),
         "bt_msp_batch": ([P, P, u32, i32, P, P], i32),
         "bt_ebfc_batch": ([P, P, u32, P, P], i32),
         "bt_ctx_memory_peak": ([P, C.POINTER(u64), i32], i32),
@@ -320,6 +321,10 @@ class Context:
         ms = C.c_double()
         _check(load().bt_msp_autotune(self._c, _ptr(a), C.byref(ms)), "msp autotune")
         return tuple(int(x) for x in a), ms.value
+
+    def set_peel_ctas(self, ctas: int) -> None:
+        """CTAs of the peeling kernel (0: one per SM, the whole GPU)."""
+        _check(load().bt_ctx_set_peel_ctas(self._c, ctas), "set_peel_ctas")
 
     # batched arenas ----------------------------------------------------------
     def set_arena_edges(self, edges: int) -> None:

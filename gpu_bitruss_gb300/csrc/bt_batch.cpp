@@ -158,6 +158,12 @@ extern "C" bt_status bt_graph_pack(const bt_graph *const *graphs, uint32_t count
     return BT_OK;
 }
 
+extern "C" bt_status bt_ctx_set_peel_ctas(bt_ctx *ctx, uint32_t ctas) {
+    if (!ctx) return bt_fail(BT_ERR_INVALID, "null context");
+    ctx->peel_ctas = ctas;
+    return BT_OK;
+}
+
 extern "C" bt_status bt_ctx_set_arena_edges(bt_ctx *ctx, uint64_t edges) {
     if (!ctx) return bt_fail(BT_ERR_INVALID, "null context");
     if (edges == 0 || edges > kMaxArenaEdges) return bt_fail(BT_ERR_INVALID, "arena edges must be in [1, 2^31-1]");

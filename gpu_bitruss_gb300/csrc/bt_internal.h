@@ -133,6 +133,7 @@ struct bt_ctx {
     // msp task schedule (0 = built-in value): min grain, tasks per CTA, local-plan limit
     uint32_t msp_schedule[3] = {0, 0, 0};
     uint64_t arena_edges = 1ull << 28;  // batched calls: edges per arena, at most
+    uint32_t peel_ctas = 0;             // CTAs of the peeling kernel (0 = one per SM)
 };
 
 // Default msp task schedule (bt_ctx_set_msp_schedule with 0 picks these):

@@ -48,6 +48,7 @@
 // the kernel returns.
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <mutex>
 #include <type_traits>
 
@@ -725,7 +726,45 @@ __global__ void k_two_hop(MspArgs a) { compute_two_hop(a); }
 
 }  // namespace
 
-static std::mutex g_coop_mutex;
+// CTA slots of the peeling kernel, per device.  A cooperative peel holds
+// `nblocks` slots from its launch until it has finished; the slots of a device
+// add up to what the device keeps resident at once (one CTA per SM), so the
+// peels that run together -- contexts with a share of the SMs each, such as
+// serving slots -- always fit side by side and never wait at a grid barrier for
+// CTAs that cannot be placed.  A peel that wants every SM waits for the
+// others to finish.
+namespace {
+constexpr int kMaxPoolDevices = 64;
+std::mutex g_pool_mu;
+std::condition_variable g_pool_cv;
+int g_pool_free[kMaxPoolDevices];
+bool g_pool_init[kMaxPoolDevices];
+
+struct CtaSlots {
+    int dev = -1, n = 0;
+    void acquire(int device, int capacity, int want) {
+        std::unique_lock<std::mutex> lk(g_pool_mu);
+        if (!g_pool_init[device]) {
+            g_pool_free[device] = capacity;
+            g_pool_init[device] = true;
+        }
+        g_pool_cv.wait(lk, [&] { return g_pool_free[device] >= want; });
+        g_pool_free[device] -= want;
+        dev = device;
+        n = want;
+    }
+    void release() {
+        if (n == 0) return;
+        {
+            std::lock_guard<std::mutex> lk(g_pool_mu);
+            g_pool_free[dev] += n;
+            n = 0;
+        }
+        g_pool_cv.notify_all();
+    }
+    ~CtaSlots() { release(); }
+};
+}  // namespace
 
 static unsigned long long wait_limit_ns() {
     const char *us = getenv("BT_WAIT_LIMIT_US");
@@ -870,21 +909,23 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     int per_sm = 0;
     C(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, kThreads, smem));
     if (per_sm < 1) { release(); return bt_fail(BT_ERR_CUDA, "msp kernel does not fit on an SM"); }
-    a.nblocks = (uint32_t)(ctx->sm_count * per_sm);
-    // One cooperative peeling kernel at a time in this process: two grids that
-    // each fill the GPU could both be partly resident, each waiting at its
-    // grid barrier for CTAs that cannot be placed.  Contexts on other streams
-    // (serving slots) still overlap their counting, uploads and copies.
-    std::unique_lock<std::mutex> coop(g_coop_mutex, std::defer_lock);
+    const uint32_t capacity = (uint32_t)(ctx->sm_count * per_sm);
+    a.nblocks = ctx->peel_ctas && ctx->peel_ctas < capacity ? ctx->peel_ctas : capacity;
+    if (ctx->device < 0 || ctx->device >= kMaxPoolDevices) {
+        release();
+        return bt_fail(BT_ERR_INVALID, "device index out of range");
+    }
+    // CTA slots (see CtaSlots): concurrent peels of this process fit side by side
+    CtaSlots slots;
     NvtxRange range("k_msp");
     if (m) {
-        coop.lock();
+        slots.acquire(ctx->device, (int)capacity, (int)a.nblocks);
         void *params[] = {&a};
         cudaEventRecord(ctx->ev[4], st);
         cudaError_t le = cudaLaunchCooperativeKernel(kfn, dim3(a.nblocks), dim3(kThreads), params, smem, st);
         if (le == cudaSuccess) le = cudaGetLastError();
         if (le != cudaSuccess) {
-            coop.unlock();
+            slots.release();
             release();
             return bt_cuda_fail(le, "cudaLaunchCooperativeKernel(k_msp)", __FILE__, __LINE__);
         }
@@ -896,7 +937,7 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
     {
         cudaError_t ce = cudaMemcpyAsync(&h, s, sizeof(MspState), cudaMemcpyDeviceToHost, st);
         if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-        if (coop.owns_lock()) coop.unlock();
+        slots.release();
         if (ce != cudaSuccess) {
             release();
             return bt_cuda_fail(ce, "msp state readback", __FILE__, __LINE__);

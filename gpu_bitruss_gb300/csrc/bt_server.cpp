@@ -339,6 +339,9 @@ extern "C" bt_status bt_server_create(int device, uint32_t slots, uint64_t hbm_b
             for (bt_ctx *x : s->ctxs) bt_ctx_free(x);
             return rc;
         }
+        // each slot peels on its share of the SMs, so the slots' peels run
+        // side by side (bt_ctx_set_peel_ctas)
+        c->peel_ctas = std::max<uint32_t>(1u, (uint32_t)c->sm_count / slots);
         s->ctxs.push_back(c);
     }
     if (hbm_budget == 0) {

@@ -204,6 +204,15 @@ bt_status bt_graph_pack(const bt_graph *const *graphs, uint32_t count, bt_graph 
 /* Largest arena, in edges, of this context's batched calls (1 .. 2^31-1). */
 bt_status bt_ctx_set_arena_edges(bt_ctx *ctx, uint64_t edges);
 
+/* CTAs of this context's peeling kernel (0, the default: one per SM, the
+ * whole GPU).  No reference counterpart.  The peel is bound by the latency of
+ * its chain of sub-rounds rather than by the SMs' throughput, so several
+ * contexts, each with a share of the SMs, peel side by side on one GPU (the
+ * server gives each slot an equal share).  Concurrent peels of one process
+ * never hold more CTAs than the device keeps resident: a peel waits until
+ * its share is free.  Results do not depend on it. */
+bt_status bt_ctx_set_peel_ctas(bt_ctx *ctx, uint32_t ctas);
+
 /* msp (exact = 0, the reference rule) or the corrected rule (exact = 1) of
  * every graph.  bitruss: sum of m entries, graph i's edges from edge_base[i]
  * on in its own edge-id order; levels: count entries, each graph's "msp with

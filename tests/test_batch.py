@@ -175,6 +175,22 @@ def test_msp_batch_random_vs_oracle(engine, gpu_ctx, oracle_mod):
 
 
 @pytest.mark.gpu
+def test_peel_on_a_share_of_the_sms(engine, gpu_ctx):
+    """The peeling kernel on fewer CTAs than SMs gives the same results."""
+    gd = load_golden("cl20k")
+    g = engine.Graph.from_edges(gd["u"], gd["v"])
+    gpu_ctx.upload(g)
+    try:
+        for ctas in (1, 7, 38, 76, 100000):
+            gpu_ctx.set_peel_ctas(ctas)
+            b, lv = gpu_ctx.msp()
+            np.testing.assert_array_equal(b.astype(np.uint64), gd["msp"])
+            assert lv == int(gd["levels"])
+    finally:
+        gpu_ctx.set_peel_ctas(0)
+
+
+@pytest.mark.gpu
 def test_msp_batch_empty(engine, gpu_ctx):
     res, levels = gpu_ctx.msp_batch([])
     assert res == [] and len(levels) == 0

@@ -41,6 +41,30 @@ def test_cl20m_counts_and_decomposition(engine, gpu_ctx):
         assert gpu_ctx.stats()[1] == want["subrounds"]
 
 
+def test_cl20m_hidx(engine, gpu_ctx):
+    """Config 2's h-index bitruss numbers at full size.  The iteration starts
+    from the exact peel's values (more than 2^20 edges) and verifies them in
+    one round that changes nothing; the result must equal the oracle's true
+    bitruss numbers (its exact peel, tests/golden/cl20m.json) when recorded,
+    else the exact peel run here."""
+    from gpu_bitruss_gb300 import gen
+    with open(os.path.join(GOLDEN, "cl20m.json")) as f:
+        want = json.load(f)
+    u, v = gen.by_name("cl20m")
+    g = engine.Graph.from_edges(u, v)
+    gpu_ctx.upload(g)
+    h, rounds = gpu_ctx.hidx()
+    st = gpu_ctx.stats()
+    assert st[19] == 1 and rounds == 1 and st[18] == g.m
+    digest = hashlib.sha256(h.astype("<u4").tobytes()).hexdigest()
+    if "exact_sha256" in want:
+        assert digest == want["exact_sha256"]
+    else:
+        x, _ = gpu_ctx.msp(exact=True)
+        assert np.array_equal(h, x)
+    assert int(h.max()) == want.get("exact_levels", int(h.max()))
+
+
 def test_hub100m_counts(engine):
     """Config 3 at full size (hub-skewed, 100M edges, hubs of ~10^6
     neighbours): butterfly count, largest support and the digest of all 100M
