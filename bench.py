@@ -98,9 +98,9 @@ def load_peaks():
 
 # DRAM bytes per k_msp launch, measured by ncu on graphs larger than L2 but
 # small enough to capture (profiles/k_msp_dram_traffic.md).  The traffic per
-# row position grows with the graph (2M edges: 1.27 B, 5M: 10.85 B), so it is
+# row position grows with the graph (2M edges: 1.17 B, 5M: 10.57 B), so it is
 # not scaled to other sizes: other workloads report none.
-DRAM_TRAFFIC = {"cl2000k": 16_232_689_408 + 2_250_057_728, "cl5000k": 624_777_743_872 + 71_806_630_400}
+DRAM_TRAFFIC = {"cl2000k": 14_827_734_272 + 2_185_049_344, "cl5000k": 608_334_618_112 + 70_095_516_672}
 
 
 def load_traffic(workload):
@@ -389,9 +389,22 @@ def batch_graphs(workload: str, rank: int = 0):
     import gpu_bitruss_gb300 as bt
     count = int(workload[len("batch"):])
     sizes = gen.batch_sizes()
-    lists = [gen.batch_graph(i, sizes=sizes) for i in batch_shard(count, rank, total=len(sizes[0]))]
+    idx = batch_shard(count, rank, total=len(sizes[0]))
+    if len(idx) > 64:
+        # many graphs: generate them in a process pool (spawned, and before
+        # this process touches the GPU)
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+            lists = pool.map(_batch_graph, idx, chunksize=4)
+    else:
+        lists = [gen.batch_graph(i, sizes=sizes) for i in idx]
     graphs = [bt.Graph.from_edges(u, v) for u, v in lists]
     return graphs, lists
+
+
+def _batch_graph(i):
+    from gpu_bitruss_gb300 import gen
+    return gen.batch_graph(i)
 
 
 def run_batch(args):

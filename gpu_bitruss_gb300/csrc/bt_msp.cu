@@ -726,13 +726,13 @@ __global__ void k_two_hop(MspArgs a) { compute_two_hop(a); }
 
 }  // namespace
 
-// CTA slots of the peeling kernel, per device.  A cooperative peel holds
-// `nblocks` slots from its launch until it has finished; the slots of a device
-// add up to what the device keeps resident at once (one CTA per SM), so the
-// peels that run together -- contexts with a share of the SMs each, such as
-// serving slots -- always fit side by side and never wait at a grid barrier for
-// CTAs that cannot be placed.  A peel that wants every SM waits for the
-// others to finish.
+// SM slots of the peeling kernel, per device.  A cooperative peel of nblocks
+// CTAs (per_sm resident per SM) holds ceil(nblocks / per_sm) slots from its
+// launch until it has finished; a device has one slot per SM, so the peels
+// that run together -- contexts with a share of the SMs each, such as serving
+// slots -- always fit side by side and never wait at a grid barrier for CTAs
+// that cannot be placed.  A peel that wants every SM waits for the others to
+// finish.
 namespace {
 constexpr int kMaxPoolDevices = 64;
 std::mutex g_pool_mu;
@@ -915,11 +915,11 @@ bt_status dev_msp(bt_ctx *ctx, bool exact, uint32_t *levels) {
         release();
         return bt_fail(BT_ERR_INVALID, "device index out of range");
     }
-    // CTA slots (see CtaSlots): concurrent peels of this process fit side by side
+    // SM slots (see CtaSlots): concurrent peels of this process fit side by side
     CtaSlots slots;
     NvtxRange range("k_msp");
     if (m) {
-        slots.acquire(ctx->device, (int)capacity, (int)a.nblocks);
+        slots.acquire(ctx->device, ctx->sm_count, (int)((a.nblocks + per_sm - 1) / per_sm));
         void *params[] = {&a};
         cudaEventRecord(ctx->ev[4], st);
         cudaError_t le = cudaLaunchCooperativeKernel(kfn, dim3(a.nblocks), dim3(kThreads), params, smem, st);
