@@ -36,44 +36,59 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-struct Barrier {
-    unsigned count, gen, abort, error;
+// gen and abort share one 8-byte word, so a waiting CTA reads both with one load.
+struct __align__(8) Barrier {
+    unsigned gen, abort, count, error;
 };
+
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 
 enum : unsigned { ERR_NONE = 0, ERR_TIMEOUT = 1, ERR_OVERFLOW = 2 };
 
 // All `nblocks` CTAs of a cooperative grid meet here.  The wait is bounded by
 // `wait_ns` of wall time; when it expires the CTA records ERR_TIMEOUT, raises
 // `abort` and returns false, and every other waiting CTA returns false too.
+// Thread 0 reads the generation before the block has synchronised: it cannot
+// advance until this CTA has arrived, so the read overlaps the CTA's last work.
 __device__ inline bool grid_barrier(Barrier *b, unsigned nblocks, unsigned long long wait_ns) {
     __shared__ int s_ok;
+    const unsigned long long *word = reinterpret_cast<const unsigned long long *>(&b->gen);
+    unsigned gen = 0;
+    if (threadIdx.x == 0) gen = ld_acquire(&b->gen);
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        unsigned gen = ld_acquire(&b->gen);
         __threadfence();
         unsigned arrived = atomicAdd(&b->count, 1u) + 1;
         if (arrived == nblocks) {
             b->count = 0;
             __threadfence();
             st_release(&b->gen, gen + 1);
+            if (ld_acquire(&b->abort)) ok = 0;
         } else {
-            unsigned long long t0 = global_ns();
+            unsigned long long t0 = 0;
             unsigned sleep = 32;
-            while (ld_acquire(&b->gen) == gen) {
-                if (ld_acquire(&b->abort)) { ok = 0; break; }
-                if (global_ns() - t0 > wait_ns) {
+            for (;;) {
+                const unsigned long long w = ld_acquire64(word);  // (abort << 32) | gen
+                if ((unsigned)(w >> 32)) { ok = 0; break; }
+                if ((unsigned)w != gen) break;
+                const unsigned long long t = global_ns();
+                if (!t0) t0 = t;
+                else if (t - t0 > wait_ns) {
                     atomicCAS(&b->error, 0u, (unsigned)ERR_TIMEOUT);
                     atomicExch(&b->abort, 1u);
                     ok = 0;
                     break;
                 }
                 __nanosleep(sleep);
-                if (sleep < 256) sleep <<= 1;
+                if (sleep < 128) sleep <<= 1;
             }
         }
         __threadfence();
-        if (ld_acquire(&b->abort)) ok = 0;
         s_ok = ok;
     }
     __syncthreads();
