@@ -426,12 +426,18 @@ def run_batch(args):
     ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=f"cuda:{local}")
 
-    # autotune the peel schedule on a sample arena (every 8th graph)
+    # the peel schedule: --schedule, else autotuned on a sample arena (every 8th graph)
     sample = graphs[::8]
-    arena_s, _ = bt.pack(sample)
-    ctx.upload(arena_s)
     t_tune = time.perf_counter()
-    sched, tune_ms = ctx.autotune()
+    if args.schedule:
+        ctx.set_msp_schedule(*[int(x) for x in args.schedule.split(",")])
+        sched, tuned_on = ctx.msp_schedule(), "given (--schedule)"
+    else:
+        arena_s, _ = bt.pack(sample)
+        ctx.upload(arena_s)
+        sched, tune_ms = ctx.autotune()
+        del arena_s
+        tuned_on = f"every 8th graph ({len(sample)} graphs, {int(sum(g.m for g in sample))} edges)"
     t_tune = time.perf_counter() - t_tune
 
     # the arena resident in HBM
@@ -498,7 +504,7 @@ def run_batch(args):
                    "l2": "512 MB flush between timed steps; arena > L2",
                    "subrounds": stats[1], "levels": stats[0], "peel_ms": statistics.median(peel_ms),
                    "schedule": {"min_grain": sched[0], "tasks_per_cta": sched[1], "local_plan": sched[2],
-                                "tuned_on": f"every 8th graph ({len(sample)} graphs, {int(arena_s.m)} edges)",
+                                "tuned_on": tuned_on,
                                 "tune_s": round(t_tune, 2)},
                    "gen_s": round(t_gen, 1)},
         "e2e": {"value": world * count * args.steps / (e2e_ms / 1000.0), "unit": "graphs/s",

@@ -70,15 +70,15 @@ struct DeviceGuard {
 // out (the library does not link the driver library itself).
 bt_status current_context(CUcontext *out) {
     using GetCurrent = CUresult (*)(CUcontext *);
-    static GetCurrent fn = nullptr;
-    if (!fn) {
+    // looked up once; a function-local static is initialised thread-safely
+    static const GetCurrent fn = []() -> GetCurrent {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q{};
         cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q);
-        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
-            return bt_fail(BT_ERR_CUDA, "cuCtxGetCurrent is not available from the CUDA driver");
-        fn = reinterpret_cast<GetCurrent>(p);
-    }
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess) return nullptr;
+        return reinterpret_cast<GetCurrent>(p);
+    }();
+    if (!fn) return bt_fail(BT_ERR_CUDA, "cuCtxGetCurrent is not available from the CUDA driver");
     *out = nullptr;
     if (fn(out) != CUDA_SUCCESS || !*out) return bt_fail(BT_ERR_CUDA, "no current CUDA context");
     return BT_OK;
