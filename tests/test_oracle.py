@@ -170,6 +170,27 @@ def test_table_form_equals_merge_form(oracle_mod, shape):
         b, lb, sb = oracle_mod.msp(g, 4, table_mode, sup)
         np.testing.assert_array_equal(a, b)
         assert la == lb and sa[1] == sb[1]
+        # the algorithmic bytes count the reference's own walk, whichever form
+        # of the oracle visits the butterflies: row bytes, butterflies visited
+        # (all four edges live) and unit decrements are the same
+        assert sa[4:8] == sb[4:8]
+        assert sa[7] == sa[4] + 8 * sa[5] + 8 * sa[6]
+
+
+def test_algorithmic_bytes_by_hand():
+    """The reference walk's byte count on K(2,2) (one butterfly, m = 4).
+    Supports are all 1, so level 1 peels all four edges in one sub-round.
+    Every peeled edge (u, v) reads u's row (2 live neighbours, 4 B each), v's
+    row with edge ids (2 x 8 B) and the row of the one other w in N(v)
+    (2 x 4 B): 32 B per edge, 128 B.  Each edge visits the butterfly once
+    (all four edges live at the start of the sub-round): 4 visits.  All three
+    other edges are in the frontier, so the rule decrements nothing."""
+    from oracle import oracle as O
+    g = O.build_csr(np.array([0, 0, 1, 1], np.uint32), np.array([0, 1, 0, 1], np.uint32))
+    for mode in (O.MSP_REF, O.MSP_TABLE):
+        res, levels, st = O.msp(g, 1, mode)
+        assert list(res) == [1, 1, 1, 1] and levels == 1
+        assert st[4:8] == [128, 4, 0, 128 + 8 * 4]
 
 
 @pytest.mark.parametrize("shape", ["cl50k", "hub"])
