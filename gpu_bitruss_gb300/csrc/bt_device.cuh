@@ -325,7 +325,10 @@ __device__ inline uint32_t warp_find_slot(const uint32_t *pre, uint32_t d, uint3
 // and hands every hit -- y != piv adjacent to both mid and anc -- to on_hit
 // right away, in two steps so that the memory traffic of a lane's hits
 // overlaps: on_hit.load(state, k, e_my, a) (loads only) for all of them,
-// on_hit.apply(state) for each, then on_hit.settle(state) for each.  k =
+// on_hit.apply(state) for each, then on_hit.settle(state) for each; after
+// each stretch the whole warp calls on_hit.stretch_done(), and on_hit.stop()
+// (the same answer across a warp, and across the block between slices) ends
+// the walk early when it returns true.  k =
 // slice slot of mid (| kRevHit for a reverse hit), e_my = the edge id
 // (mid, y), a = the anchor's answer for y (walk_lookup's convention: a hash
 // slot when anc is staged, else the edge id).  settle acts on the results of
@@ -401,6 +404,7 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
         // (kPerThread consecutive ones per lane) and act on their own hits
         // at once: no block-wide synchronisation until the slice is done.
         for (uint32_t wb = warp * (32 * kPerThread); wb < tot; wb += kRound) {
+            if (on_hit.stop()) break;  // warp-uniform
             uint32_t hk[kPerThread], hp[kPerThread], ha[kPerThread];
             uint32_t hitmask = 0, act = 0, rev = 0;
             uint32_t jp[kPerThread], yv[kPerThread], ev[kPerThread];
@@ -479,12 +483,14 @@ __device__ __forceinline__ void walk_range(const Rows &r, const uint32_t *rowpre
 #pragma unroll
             for (uint32_t p = 0; p < kPerThread; p++)
                 if (hitmask & (1u << p)) on_hit.settle(hs[p]);
+            on_hit.stretch_done();  // the whole warp
         }
         __syncthreads();
         prof_mark(w, PF_PROBE);
         slice_done(cl, c0 + kSliceMids > s_hi);
         __syncthreads();
         prof_mark(w, PF_FLUSH);
+        if (on_hit.stop()) break;  // block-uniform: nothing changes it after the syncs
     }
 }
 

@@ -73,11 +73,16 @@ struct HidxArgs {
     unsigned *changed;
 };
 
-// pass 1 of an edge: K = list length, cge = values >= H
+// pass 1 of an edge: K = list length, cge = values >= H.  The walk stops once
+// the block has counted H values >= H (the edge keeps H whatever the rest);
+// K is then partial, which is fine: it is only used when cge < H.
 struct CountHits {
     const unsigned long long *prev;
     const bt::Walk &w;
-    unsigned long long H, K = 0, cge = 0;
+    unsigned long long H;
+    unsigned long long *live;  // shared: values >= H counted by the block so far
+    unsigned long long K = 0, cge = 0;
+    uint32_t stretch_cge = 0;
     struct State {
         unsigned long long p1, p2, p3;
     };
@@ -91,9 +96,22 @@ struct CountHits {
         unsigned long long v = s.p1 < s.p2 ? s.p1 : s.p2;
         v = v < s.p3 ? v : s.p3;
         K++;
-        if (v >= H) cge++;
+        if (v >= H) {
+            cge++;
+            stretch_cge++;
+        }
     }
     __device__ __forceinline__ void settle(const State &) const {}
+    __device__ __forceinline__ void stretch_done() {
+        const uint32_t c = __reduce_add_sync(0xffffffffu, stretch_cge);
+        stretch_cge = 0;
+        if ((threadIdx.x & 31) == 0 && c) atomicAdd(live, (unsigned long long)c);
+    }
+    __device__ __forceinline__ bool stop() const {
+        unsigned long long v = 0;
+        if ((threadIdx.x & 31) == 0) v = *reinterpret_cast<volatile unsigned long long *>(live);
+        return __shfl_sync(0xffffffffu, v, 0) >= H;
+    }
 };
 
 // a refinement pass: histogram of the values in [lo, hi), count of those >= hi
@@ -118,6 +136,8 @@ struct BinHits {
         else if (v >= lo) atomicAdd(&hist[(v - lo) / width], 1u);
     }
     __device__ __forceinline__ void settle(const State &) const {}
+    __device__ __forceinline__ void stretch_done() const {}
+    __device__ __forceinline__ bool stop() const { return false; }  // a histogram needs every value
 };
 
 struct HSmem {
@@ -125,6 +145,7 @@ struct HSmem {
     uint32_t hist[kBuckets];
     unsigned long long red[2][kThreads / 32];
     unsigned long long e0;
+    unsigned long long live;  // pass 1: values >= H counted so far (early stop)
     unsigned long long win_lo, win_hi, above, result;
     int done;
 };
@@ -179,9 +200,11 @@ __global__ void __launch_bounds__(kThreads) k_hidx_round(HidxArgs a) {
             const uint32_t cu = a.two_hop[uv.x], cv = a.two_hop[uv.y];
             const uint32_t piv = cv <= cu ? uv.y : uv.x, anc = cv <= cu ? uv.x : uv.y;
             const uint32_t total = a.two_hop[piv];
-            // pass 1: K = list length, cge = values >= H
+            // pass 1: K = list length, cge = values >= H (stops at H of them);
+            // the reset is seen by every thread after walk_range's first sync
             bt::Walk &w = sm.walk;
-            CountHits ch{prev, w, H};
+            if (threadIdx.x == 0) sm.live = 0;
+            CountHits ch{prev, w, H, &sm.live};
             bt::walk_range(a.rows, a.rowpre, w, piv, anc, 0, total, 0, total, keep_all, ch, no_slice);
             unsigned long long K = ch.K, cge = ch.cge;
             block_sum2(sm, K, cge);

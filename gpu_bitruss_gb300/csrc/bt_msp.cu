@@ -366,6 +366,8 @@ struct MspHit {
         if (s.x_my) dec_settle(a, rd, s.e_my, 1, s.x_my);
         if (s.x_ay) dec_settle(a, rd, s.e_ay, 1, s.x_ay);
     }
+    __device__ __forceinline__ void stretch_done() const {}
+    __device__ __forceinline__ bool stop() const { return false; }  // a peel walks every butterfly
 };
 
 template <bool N32>
