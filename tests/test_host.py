@@ -51,6 +51,20 @@ def test_duplicate_lines_are_kept_like_the_reference(engine, oracle_mod):
         np.testing.assert_array_equal(getattr(g, k), o[k])
 
 
+@pytest.mark.parametrize("name", ["hub500k", "cl200k"])
+def test_host_csr_equals_the_oracle_on_large_graphs(engine, oracle_mod, name):
+    """The engine's text-order CSR (process_graph numbering, reference edge
+    ids) equals the oracle's array for array on a hub-skewed graph (rows up to
+    ~10^4 long) and a power-law graph."""
+    from gpu_bitruss_gb300 import gen
+    u, v = gen.by_name(name)
+    g = engine.Graph.from_edges(u, v)
+    o = oracle_mod.build_csr(u, v)
+    assert (g.u_num, g.l_num, g.n, g.m) == (o["u_num"], o["l_num"], o["n"], o["m"])
+    for key in ("offsets", "degrees", "neighbors", "edges", "edge_ids"):
+        np.testing.assert_array_equal(getattr(g, key), o[key], err_msg=key)
+
+
 def test_empty_graph(engine):
     g = engine.Graph.from_edges(np.zeros(0, np.uint32), np.zeros(0, np.uint32))
     assert (g.n, g.m) == (0, 0)
